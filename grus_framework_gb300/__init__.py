@@ -1,0 +1,304 @@
+"""grus_framework_gb300 -- GB300-native frontier-traversal core (Grus drop-in).
+
+Python host side over the C ABI in include/grus.h (libgrus.so, hand-written
+sm_103a CUDA).  There is no CPU fallback: importing the package loads the
+library and raises if it has not been built (``__graft_entry__.build()`` or
+``python -m grus_framework_gb300.build``).
+
+The names follow the reference's interface: a graph is loaded from a Galois
+``.gr`` file (graph_loader::Load, include/graph_loader.cuh:160-166) or built
+from CSR arrays, and the per-application operators (BFS, SSSP, CC, PageRank)
+run over it on the device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libgrus.so"
+
+INFINIT = 4294967294
+OK, ENOENT, EIO, ENOMEM, EBUSY, ENODEV, EINVAL, EOVERFLOW, ETIMEDOUT, ECUDA = (
+    0, -2, -5, -12, -16, -19, -22, -75, -110, -1000)
+MEM_DEVICE, MEM_MANAGED = 0, 1
+GRAPH_SYMMETRIC, GRAPH_WEIGHTED = 1, 2
+GEN_SYMMETRIC, GEN_WEIGHTED, GEN_RELABEL = 1, 2, 4
+
+
+class GrusError(RuntimeError):
+    def __init__(self, status: int, what: str, detail: str = ""):
+        self.status = status
+        msg = f"{what}: {_strerror(status)} ({status})"
+        if detail:
+            msg += f": {detail}"
+        super().__init__(msg)
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("levels", C.c_uint32),
+        ("bottom_up_levels", C.c_uint32),
+        ("direction_switches", C.c_uint32),
+        ("kernel_launches", C.c_uint32),
+        ("vertices_reached", C.c_uint64),
+        ("edges_reached", C.c_uint64),
+        ("edges_relaxed", C.c_uint64),
+        ("device_ms", C.c_float),
+        ("reserved0", C.c_uint32),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}
+
+
+class GraphInfo(C.Structure):
+    _fields_ = [
+        ("n", C.c_uint64), ("m", C.c_uint64),
+        ("max_degree_vertex", C.c_uint32), ("max_degree", C.c_uint32),
+        ("flags", C.c_uint32), ("mem_mode", C.c_int32),
+        ("offsets", C.c_void_p), ("cols", C.c_void_p), ("weights", C.c_void_p),
+        ("t_offsets", C.c_void_p), ("t_cols", C.c_void_p), ("t_weights", C.c_void_p),
+        ("budget_bytes", C.c_uint64),
+    ]
+
+
+class Tuning(C.Structure):
+    _fields_ = [
+        ("alpha", C.c_float), ("beta", C.c_float), ("ctas_per_sm", C.c_uint32),
+        ("huge_degree", C.c_uint32), ("bu_scan", C.c_uint32), ("timeout_ms", C.c_uint32),
+    ]
+
+
+def _load():
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"libgrus.so not built at {LIB_PATH}; run __graft_entry__.build() "
+            "(the package has no CPU fallback)")
+    L = C.CDLL(str(LIB_PATH))
+    vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+    PG = C.POINTER(vp)
+    sig = {
+        "grus_version": ([], C.c_char_p),
+        "grus_strerror": ([i32], C.c_char_p),
+        "grus_last_error": ([], C.c_char_p),
+        "grus_device_init": ([i32], i32),
+        "grus_graph_from_csr": ([u64, u64, vp, vp, vp, u32, i32, u64, PG], i32),
+        "grus_graph_load_gr": ([C.c_char_p, i32, i32, u64, PG], i32),
+        "grus_graph_save_gr": ([vp, C.c_char_p], i32),
+        "grus_graph_rmat": ([i32, i32, u64, u32, i32, u64, PG], i32),
+        "grus_graph_grid2d": ([u32, u32, u64, u32, PG], i32),
+        "grus_graph_get_info": ([vp, C.POINTER(GraphInfo)], i32),
+        "grus_graph_copy_csr": ([vp, vp, vp, vp], i32),
+        "grus_graph_build_csc": ([vp], i32),
+        "grus_graph_copy_csc": ([vp, vp, vp, vp], i32),
+        "grus_graph_set_tuning": ([vp, C.POINTER(Tuning)], i32),
+        "grus_graph_get_tuning": ([vp, C.POINTER(Tuning)], i32),
+        "grus_graph_free": ([vp], i32),
+        "grus_bfs": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    return L
+
+
+lib = _load()
+
+
+def _strerror(status):
+    return lib.grus_strerror(status).decode()
+
+
+def _check(status, what):
+    if status != 0:
+        raise GrusError(status, what, lib.grus_last_error().decode())
+
+
+def version() -> str:
+    return lib.grus_version().decode()
+
+
+def device_init(device: int = 0) -> None:
+    _check(lib.grus_device_init(device), "grus_device_init")
+
+
+def _ptr(buf):
+    """Address of a numpy array, torch tensor or raw integer pointer."""
+    if buf is None:
+        return None
+    if isinstance(buf, int):
+        return buf
+    if isinstance(buf, np.ndarray):
+        if not buf.flags["C_CONTIGUOUS"]:
+            raise ValueError("buffer must be C-contiguous")
+        return buf.ctypes.data
+    if hasattr(buf, "data_ptr"):
+        if not buf.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return buf.data_ptr()
+    raise TypeError(f"unsupported buffer type {type(buf)!r}")
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return getattr(stream, "cuda_stream", None)
+
+
+class Graph:
+    """A device-resident CSR graph (uint32 offsets, columns and weights)."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle)
+
+    # ---- construction -----------------------------------------------------
+    @classmethod
+    def rmat(cls, scale, edge_factor=16, seed=1, symmetric=True, weighted=False,
+             relabel=True, managed=False, budget_bytes=0):
+        flags = ((GEN_SYMMETRIC if symmetric else 0) | (GEN_WEIGHTED if weighted else 0)
+                 | (GEN_RELABEL if relabel else 0))
+        h = C.c_void_p()
+        _check(lib.grus_graph_rmat(scale, edge_factor, seed, flags,
+                                   MEM_MANAGED if managed else MEM_DEVICE, budget_bytes,
+                                   C.byref(h)), "grus_graph_rmat")
+        return cls(h.value)
+
+    @classmethod
+    def grid2d(cls, rows, cols, seed=0, weighted=False):
+        h = C.c_void_p()
+        _check(lib.grus_graph_grid2d(rows, cols, seed, GEN_WEIGHTED if weighted else 0,
+                                     C.byref(h)), "grus_graph_grid2d")
+        return cls(h.value)
+
+    @classmethod
+    def from_csr(cls, offsets, cols, weights=None, symmetric=False, managed=False,
+                 budget_bytes=0):
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+        cols = np.ascontiguousarray(cols, dtype=np.uint32)
+        if cols.size == 0:
+            cols = np.zeros(1, np.uint32)[:0]
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.uint32)
+        n = offsets.size - 1
+        m = int(offsets[-1]) if n >= 0 else 0
+        h = C.c_void_p()
+        _check(lib.grus_graph_from_csr(n, m, _ptr(offsets), _ptr(cols) if m else None,
+                                       _ptr(w) if w is not None else None,
+                                       GRAPH_SYMMETRIC if symmetric else 0,
+                                       MEM_MANAGED if managed else MEM_DEVICE, budget_bytes,
+                                       C.byref(h)), "grus_graph_from_csr")
+        return cls(h.value)
+
+    @classmethod
+    def load_gr(cls, path, need_weights=False, managed=False, budget_bytes=0):
+        h = C.c_void_p()
+        _check(lib.grus_graph_load_gr(str(path).encode(), int(bool(need_weights)),
+                                      MEM_MANAGED if managed else MEM_DEVICE, budget_bytes,
+                                      C.byref(h)), "grus_graph_load_gr")
+        return cls(h.value)
+
+    # ---- queries ----------------------------------------------------------
+    def _handle(self):
+        if not self._h or not self._h.value:
+            raise ValueError("graph has been freed")
+        return self._h
+
+    def info(self) -> GraphInfo:
+        inf = GraphInfo()
+        _check(lib.grus_graph_get_info(self._handle(), C.byref(inf)), "grus_graph_get_info")
+        return inf
+
+    @property
+    def n(self):
+        return self.info().n
+
+    @property
+    def m(self):
+        return self.info().m
+
+    @property
+    def max_degree_vertex(self):
+        return self.info().max_degree_vertex
+
+    @property
+    def weighted(self):
+        return bool(self.info().flags & GRAPH_WEIGHTED)
+
+    def copy_csr(self):
+        inf = self.info()
+        offs = np.empty(inf.n + 1, np.uint32)
+        cols = np.empty(max(inf.m, 1), np.uint32)
+        wts = np.empty(max(inf.m, 1), np.uint32) if inf.weights else None
+        _check(lib.grus_graph_copy_csr(self._handle(), _ptr(offs), _ptr(cols),
+                                       _ptr(wts) if wts is not None else None),
+               "grus_graph_copy_csr")
+        return offs, cols[: inf.m], (wts[: inf.m] if wts is not None else None)
+
+    def build_csc(self):
+        _check(lib.grus_graph_build_csc(self._handle()), "grus_graph_build_csc")
+
+    def copy_csc(self):
+        inf = self.info()
+        offs = np.empty(inf.n + 1, np.uint32)
+        cols = np.empty(max(inf.m, 1), np.uint32)
+        wts = np.empty(max(inf.m, 1), np.uint32) if inf.t_weights else None
+        _check(lib.grus_graph_copy_csc(self._handle(), _ptr(offs), _ptr(cols),
+                                       _ptr(wts) if wts is not None else None),
+               "grus_graph_copy_csc")
+        return offs, cols[: inf.m], (wts[: inf.m] if wts is not None else None)
+
+    def save_gr(self, path):
+        _check(lib.grus_graph_save_gr(self._handle(), str(path).encode()), "grus_graph_save_gr")
+
+    def set_tuning(self, **kw):
+        t = Tuning()
+        _check(lib.grus_graph_get_tuning(self._handle(), C.byref(t)), "grus_graph_get_tuning")
+        for k, v in kw.items():
+            setattr(t, k, v)
+        _check(lib.grus_graph_set_tuning(self._handle(), C.byref(t)), "grus_graph_set_tuning")
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        _check(lib.grus_graph_get_tuning(self._handle(), C.byref(t)), "grus_graph_get_tuning")
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
+    def free(self):
+        if self._h and self._h.value:
+            lib.grus_graph_free(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _out_array(g: Graph, out, dtype):
+    if out is None:
+        return np.empty(g.n, dtype)
+    return out
+
+
+def bfs(g: Graph, src: int, out=None, stream=None, stats: bool = False):
+    """BFS depths from `src` (uint32, INFINIT for unreached).
+
+    `out` may be a numpy array (host) or a CUDA tensor/pointer (device); with
+    a device output and stats=False the call is asynchronous on `stream`.
+    """
+    out = _out_array(g, out, np.uint32)
+    st = Stats() if stats else None
+    _check(lib.grus_bfs(g._handle(), src, _ptr(out), C.byref(st) if st is not None else None,
+                        _stream(stream)), "grus_bfs")
+    return (out, st.as_dict()) if stats else out

@@ -1,0 +1,622 @@
+// bfs.cu -- single-source BFS as ONE persistent, direction-optimising launch.
+//
+// Replaces the reference's host-driven level loop (samples/bfs/bfs.cu:135-173:
+// per level kernel<...,Frontier<BDF>> push_kernel + flag_to_wl compaction +
+// three blocking 4-byte D2H copies, include/kernel.cuh:62-80,154-165,
+// src/worklist.cu:87-93) and its static --pull variant (kernel_pull over a
+// byte-map Frontier<BITMAP>, include/kernel.cuh:18-40,124-133).
+//
+// Design (sm_103a, 152 SMs):
+//   * cooperative launch of SMs x k CTAs; levels are separated by a grid
+//     barrier whose waits are time-bounded (grus_internal.cuh); no host sync
+//     inside a traversal.
+//   * frontier state: 1-bit bitmaps (visited + three rotating frontier maps,
+//     4 * n/8 bytes, one contiguous block covered by an L2 persistence window)
+//     and a vertex queue for push levels.
+//   * push (top-down) levels, degree-binned:
+//       - degree >= huge (8192): split into 4096-edge chunks when enqueued,
+//         each chunk expanded by a whole CTA (spreads hubs over all SMs);
+//       - degree >= 256: CTA-cooperative expansion within a queue tile;
+//       - degree >= 32: warp-cooperative expansion;
+//       - degree < 32: warp scan-based gather (lanes take consecutive edges of
+//         the warp's 32 vertices, owner found by a shuffle binary search).
+//     A discovered vertex is claimed with one atomicOr on the L2-resident
+//     visited bitmap and appended with a warp-aggregated reservation.
+//   * pull (bottom-up) levels: a warp owns 32 consecutive vertices (one bitmap
+//     word); each unvisited vertex scans its first `bu_scan` neighbours four at
+//     a time and stops at the first frontier parent; longer unresolved lists
+//     are deferred to a CTA list and finished warp-cooperatively (32
+//     neighbours per ballot).  The word's next-frontier and visited bits are
+//     written with one store per warp.
+//   * direction: Beamer's heuristic -- push->pull when m_f > m_u/alpha,
+//     pull->push when n_f < n/beta and the frontier shrinks; switching back to
+//     push compacts the frontier bitmap into the binned queue.
+// Depths are order-independent (every writer stores level+1), so results are
+// bit-exact against the serial oracle whatever the schedule.
+#include <algorithm>
+#include <cstring>
+
+#include "grus_internal.cuh"
+
+namespace grus {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
+constexpr uint32_t kChunk = 4096;     // edges per chunk work item
+constexpr uint32_t kCtaTh = 256;      // CTA-cooperative degree threshold
+constexpr uint32_t kDefHuge = 8192;   // chunking threshold
+constexpr uint32_t kDefBuScan = 8;    // pull: neighbours checked before deferring
+constexpr int kDeferCap = 1024;       // pull: deferred vertices per CTA
+constexpr float kDefAlpha = 15.f, kDefBeta = 18.f;
+
+struct LevelSlot {
+  uint32_t qcount;         // queue entries of this level
+  uint32_t ccount;         // chunk entries of this level
+  uint32_t nf;             // vertices discovered into this level
+  uint32_t pad;
+  unsigned long long mf;   // sum of their out-degrees
+  unsigned long long pad2;
+};
+
+struct Summary {
+  uint32_t levels, bu_levels, switches, pad;
+  unsigned long long nr, mr;
+};
+
+struct Args {
+  const uint32_t *__restrict__ offs;
+  const uint32_t *__restrict__ cols;
+  uint32_t n, W;
+  uint64_t m;
+  uint32_t src;
+  uint32_t *depth;
+  uint32_t *visited;      // W words; fronts follow contiguously
+  uint32_t *front[3];
+  uint32_t *queue[2];
+  uint4 *chunks[2];
+  uint32_t queue_cap, chunk_cap;
+  LevelSlot *slots;       // 4 rotating slots
+  GridBarrier *bar;
+  uint32_t *err;
+  Summary *summary;
+  float alpha, beta;
+  uint32_t huge, bu_scan;
+  uint64_t timeout_ns;
+};
+
+struct Workspace {
+  uint64_t n = 0, m = 0;
+  uint32_t W = 0;
+  uint32_t *depth = nullptr;     // used when the caller's buffer is on the host
+  uint32_t *bitmaps = nullptr;   // visited + 3 fronts, 4*Wp words
+  size_t bitmap_bytes = 0;
+  uint32_t *queues = nullptr;    // 2 * n
+  uint4 *chunks = nullptr;       // 2 * chunk_cap
+  uint32_t chunk_cap = 0;
+  char *ctrl = nullptr;          // slots, barrier, err, summary
+  char *ctrl_host = nullptr;     // pinned mirror for readback
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+constexpr size_t kOffSlots = 0, kOffBar = 256, kOffErr = 320, kOffSummary = 384,
+                 kCtrlBytes = 512;
+
+void ws_free(void *p) {
+  Workspace *w = (Workspace *)p;
+  if (!w) return;
+  cudaFree(w->depth);
+  cudaFree(w->bitmaps);
+  cudaFree(w->queues);
+  cudaFree(w->chunks);
+  cudaFree(w->ctrl);
+  if (w->ctrl_host) cudaFreeHost(w->ctrl_host);
+  if (w->ev0) cudaEventDestroy(w->ev0);
+  if (w->ev1) cudaEventDestroy(w->ev1);
+  delete w;
+}
+
+int ws_get(grus_graph *g, Workspace **out) {
+  if (g->ws[kWsBfs]) {
+    *out = (Workspace *)g->ws[kWsBfs];
+    return GRUS_OK;
+  }
+  Workspace *w = new Workspace();
+  w->n = g->n;
+  w->m = g->m;
+  w->W = (uint32_t)((g->n + 31) / 32);
+  const uint64_t Wp = ((uint64_t)w->W + 31) / 32 * 32;  // 128-byte aligned maps
+  w->bitmap_bytes = 4 * Wp * 4;
+  const uint32_t huge = tune_or(g->tuning.huge_degree, kDefHuge);
+  const uint64_t cap = g->m / kChunk + g->m / std::max(huge, 1u) + 2;
+  w->chunk_cap = (uint32_t)std::min<uint64_t>(cap, 0x7FFFFFFFull);
+  cudaError_t e = cudaMalloc(&w->bitmaps, w->bitmap_bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&w->queues, 2 * std::max<uint64_t>(g->n, 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&w->chunks, 2ull * w->chunk_cap * sizeof(uint4));
+  if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaMemset(w->ctrl, 0, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaMallocHost(&w->ctrl_host, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaEventCreate(&w->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&w->ev1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ws_free(w);
+    set_last_error(std::string("bfs workspace: ") + cudaGetErrorString(e));
+    return status_from_cuda(e);
+  }
+  g->ws[kWsBfs] = w;
+  g->ws_free[kWsBfs] = ws_free;
+  *out = w;
+  return GRUS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// push-direction visit of one edge target
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void td_visit(const Args &a, uint32_t dst, uint32_t nd,
+                                         uint32_t *fnext, uint32_t *qnext,
+                                         uint4 *cnext, LevelSlot *nx,
+                                         uint32_t &nf, unsigned long long &mf) {
+  const uint32_t w = dst >> 5, bit = 1u << (dst & 31u);
+  if (__ldcg(a.visited + w) & bit) return;
+  if (atomicOr(a.visited + w, bit) & bit) return;
+  a.depth[dst] = nd;
+  atomicOr(fnext + w, bit);
+  const uint32_t b = __ldg(a.offs + dst), e = __ldg(a.offs + dst + 1);
+  const uint32_t d = e - b;
+  nf += 1;
+  mf += d;
+  if (d == 0) return;
+  if (d < a.huge) {
+    const uint32_t pos = agg_reserve(&nx->qcount);
+    if (pos < a.queue_cap) qnext[pos] = dst;
+    else atomicOr(a.err, kErrOverflow);
+  } else {
+    const uint32_t nch = (d + kChunk - 1) / kChunk;
+    const uint32_t pos = atomicAdd(&nx->ccount, nch);
+    if (pos + nch <= a.chunk_cap) {
+      for (uint32_t c = 0; c < nch; ++c)
+        cnext[pos + c] = make_uint4(dst, b + c * kChunk, min(e, b + (c + 1) * kChunk), 0u);
+    } else {
+      atomicOr(a.err, kErrOverflow);
+    }
+  }
+}
+
+// Queue an already-claimed vertex (used when converting a bitmap frontier).
+__device__ __forceinline__ void enqueue_binned(const Args &a, uint32_t v,
+                                               uint32_t *qnext, uint4 *cnext,
+                                               LevelSlot *nx) {
+  const uint32_t b = __ldg(a.offs + v), e = __ldg(a.offs + v + 1);
+  const uint32_t d = e - b;
+  if (d == 0) return;
+  if (d < a.huge) {
+    const uint32_t pos = agg_reserve(&nx->qcount);
+    if (pos < a.queue_cap) qnext[pos] = v;
+    else atomicOr(a.err, kErrOverflow);
+  } else {
+    const uint32_t nch = (d + kChunk - 1) / kChunk;
+    const uint32_t pos = atomicAdd(&nx->ccount, nch);
+    if (pos + nch <= a.chunk_cap) {
+      for (uint32_t c = 0; c < nch; ++c)
+        cnext[pos + c] = make_uint4(v, b + c * kChunk, min(e, b + (c + 1) * kChunk), 0u);
+    } else {
+      atomicOr(a.err, kErrOverflow);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// push level: binned expansion of the queue and chunk list of level L
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void td_level(const Args &a, uint32_t L,
+                                         const uint32_t *qcur, uint32_t qcount,
+                                         const uint4 *ccur, uint32_t ccount,
+                                         uint32_t *fnext, uint32_t *qnext,
+                                         uint4 *cnext, LevelSlot *nx,
+                                         uint32_t &nf, unsigned long long &mf) {
+  __shared__ uint32_t s_owner, s_beg, s_end;
+  const uint32_t nd = L + 1;
+  const uint32_t lane = lane_id();
+  for (uint32_t base = blockIdx.x * kBlock; base < qcount; base += gridDim.x * kBlock) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t beg = 0, end = 0;
+    if (i < qcount) {
+      const uint32_t v = __ldcg(qcur + i);
+      beg = __ldg(a.offs + v);
+      end = __ldg(a.offs + v + 1);
+    }
+    // CTA-cooperative: one vertex at a time, whole block strides its list
+    while (true) {
+      if (threadIdx.x == 0) s_owner = 0xFFFFFFFFu;
+      __syncthreads();
+      if (end - beg >= kCtaTh) s_owner = threadIdx.x;
+      __syncthreads();
+      const uint32_t owner = s_owner;
+      if (owner == 0xFFFFFFFFu) break;
+      if (threadIdx.x == owner) {
+        s_beg = beg;
+        s_end = end;
+        beg = end;
+      }
+      __syncthreads();
+      const uint32_t cb = s_beg, ce = s_end;
+      for (uint32_t x = cb + threadIdx.x; x < ce; x += kBlock)
+        td_visit(a, __ldg(a.cols + x), nd, fnext, qnext, cnext, nx, nf, mf);
+      __syncthreads();
+    }
+    // warp-cooperative
+    while (true) {
+      const uint32_t ball = __ballot_sync(0xffffffffu, end - beg >= 32);
+      if (!ball) break;
+      const int leader = __ffs(ball) - 1;
+      const uint32_t wb = __shfl_sync(0xffffffffu, beg, leader);
+      const uint32_t we = __shfl_sync(0xffffffffu, end, leader);
+      if ((int)lane == leader) beg = end;
+      for (uint32_t x = wb + lane; x < we; x += 32)
+        td_visit(a, __ldg(a.cols + x), nd, fnext, qnext, cnext, nx, nf, mf);
+    }
+    // scan-based gather over the warp's remaining short lists
+    const uint32_t deg = end - beg;
+    uint32_t incl = deg;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += t;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      int j = 0;
+#pragma unroll
+      for (int step = 16; step >= 1; step >>= 1) {
+        const uint32_t pv = __shfl_sync(0xffffffffu, incl, j + step - 1);
+        if (pv <= k) j += step;
+      }
+      const uint32_t ob = __shfl_sync(0xffffffffu, beg, j);
+      const uint32_t oi = __shfl_sync(0xffffffffu, incl, j);
+      const uint32_t od = __shfl_sync(0xffffffffu, deg, j);
+      if (k < total) {
+        const uint32_t x = ob + (k - (oi - od));
+        td_visit(a, __ldg(a.cols + x), nd, fnext, qnext, cnext, nx, nf, mf);
+      }
+    }
+  }
+  // chunks of huge vertices: one CTA per 4096-edge chunk
+  for (uint32_t c = blockIdx.x; c < ccount; c += gridDim.x) {
+    const uint4 ch = __ldcg(ccur + c);
+    for (uint32_t x = ch.y + threadIdx.x; x < ch.z; x += kBlock)
+      td_visit(a, __ldg(a.cols + x), nd, fnext, qnext, cnext, nx, nf, mf);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pull level
+// ---------------------------------------------------------------------------
+struct PullShared {
+  uint32_t ndef;
+  uint4 def[kDeferCap];  // (v, next edge, end, begin)
+};
+
+__device__ __forceinline__ void bu_drain(const Args &a, PullShared &sh, uint32_t nd,
+                                         const uint32_t *fcur, uint32_t *fnext,
+                                         uint32_t &nf, unsigned long long &mf) {
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  const uint32_t cnt = min(sh.ndef, (uint32_t)kDeferCap);
+  for (uint32_t j = warp; j < cnt; j += kWarps) {
+    const uint4 d = sh.def[j];
+    bool hit = false;
+    for (uint32_t base = d.y; base < d.z; base += 32) {
+      const uint32_t x = base + lane;
+      const bool h = x < d.z && test_bit(fcur, __ldg(a.cols + x));
+      if (__ballot_sync(0xffffffffu, h)) {
+        hit = true;
+        break;
+      }
+    }
+    if (hit && lane == 0) {
+      const uint32_t v = d.x, bit = 1u << (v & 31u);
+      a.depth[v] = nd;
+      atomicOr(a.visited + (v >> 5), bit);
+      atomicOr(fnext + (v >> 5), bit);
+      nf += 1;
+      mf += d.z - d.w;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sh.ndef = 0;
+  __syncthreads();
+}
+
+__device__ __forceinline__ void bu_level(const Args &a, PullShared &sh, uint32_t L,
+                                         const uint32_t *fcur, uint32_t *fnext,
+                                         uint32_t &nf, unsigned long long &mf) {
+  const uint32_t nd = L + 1;
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  const uint32_t scan = a.bu_scan;
+  for (uint32_t tile = blockIdx.x; tile * kWarps < a.W; tile += gridDim.x) {
+    const uint32_t w = tile * kWarps + warp;
+    if (w < a.W) {
+      const uint32_t vis = __ldcg(a.visited + w);
+      if (vis != 0xFFFFFFFFu) {
+        const uint32_t v = w * 32 + lane;
+        const bool active = !((vis >> lane) & 1u) && v < a.n;
+        bool found = false;
+        uint32_t b = 0, e = 0;
+        if (active) {
+          b = __ldg(a.offs + v);
+          e = __ldg(a.offs + v + 1);
+          const uint32_t lim = min(e, b + scan);
+          uint32_t x = b;
+          for (; x < lim; x += 4) {
+            // four independent loads in flight, then four bitmap probes
+            uint32_t u0 = __ldg(a.cols + x);
+            uint32_t u1 = x + 1 < lim ? __ldg(a.cols + x + 1) : u0;
+            uint32_t u2 = x + 2 < lim ? __ldg(a.cols + x + 2) : u0;
+            uint32_t u3 = x + 3 < lim ? __ldg(a.cols + x + 3) : u0;
+            if (test_bit(fcur, u0) | test_bit(fcur, u1) | test_bit(fcur, u2) |
+                test_bit(fcur, u3)) {
+              found = true;
+              break;
+            }
+          }
+          if (!found && lim < e) {
+            const uint32_t pos = atomicAdd(&sh.ndef, 1u);
+            if (pos < (uint32_t)kDeferCap) {
+              sh.def[pos] = make_uint4(v, lim, e, b);
+            } else {
+              for (x = lim; x < e; ++x)
+                if (test_bit(fcur, __ldg(a.cols + x))) {
+                  found = true;
+                  break;
+                }
+            }
+          }
+        }
+        const uint32_t mask = __ballot_sync(0xffffffffu, found);
+        if (mask) {
+          if (lane == 0) {
+            a.visited[w] = vis | mask;
+            fnext[w] = mask;
+          }
+          if (found) {
+            a.depth[v] = nd;
+            nf += 1;
+            mf += e - b;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (sh.ndef > (uint32_t)(kDeferCap - kBlock)) bu_drain(a, sh, nd, fcur, fnext, nf, mf);
+  }
+  __syncthreads();
+  bu_drain(a, sh, nd, fcur, fnext, nf, mf);
+}
+
+// pull -> push: turn the next-frontier bitmap into the binned queue
+__device__ __forceinline__ void bitmap_to_queue(const Args &a, const uint32_t *fmap,
+                                                uint32_t *qnext, uint4 *cnext,
+                                                LevelSlot *nx) {
+  const uint32_t lane = lane_id();
+  const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kBlock) >> 5;
+  for (uint32_t w = gw; w < a.W; w += nw) {
+    const uint32_t word = __ldcg(fmap + w);
+    if (word && ((word >> lane) & 1u)) enqueue_binned(a, w * 32 + lane, qnext, cnext, nx);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
+  __shared__ PullShared sh;
+  const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
+  const uint32_t nthreads = gridDim.x * kBlock;
+  if (threadIdx.x == 0) sh.ndef = 0;
+  // prologue: clear the bitmaps and the level slots
+  {
+    uint32_t *bm = a.visited;
+    const uint32_t words = (uint32_t)(a.front[2] - a.visited) + a.W;
+    for (uint32_t i = gtid; i < words; i += nthreads) bm[i] = 0u;
+    if (gtid < 4 * sizeof(LevelSlot) / 4) ((uint32_t *)a.slots)[gtid] = 0u;
+  }
+  if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+  const uint32_t sb = __ldg(a.offs + a.src), se = __ldg(a.offs + a.src + 1);
+  if (gtid == 0) {
+    const uint32_t w = a.src >> 5, bit = 1u << (a.src & 31u);
+    a.visited[w] = bit;
+    a.front[0][w] = bit;
+    a.depth[a.src] = 0;
+    enqueue_binned(a, a.src, a.queue[0], a.chunks[0], a.slots);
+  }
+  if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+
+  uint32_t L = 0;
+  bool bu = false;
+  uint64_t mu = a.m - (uint64_t)(se - sb);
+  uint32_t prev_nf = 1, bu_levels = 0, switches = 0;
+  unsigned long long nr = 1, mr = se - sb;
+  while (true) {
+    LevelSlot *cur = a.slots + (L & 3u);
+    LevelSlot *nx = a.slots + ((L + 1) & 3u);
+    uint32_t *fcur = a.front[L % 3];
+    uint32_t *fnext = a.front[(L + 1) % 3];
+    uint32_t *fclr = a.front[(L + 2) % 3];
+    for (uint32_t i = gtid; i < a.W; i += nthreads) fclr[i] = 0u;
+    if (gtid < sizeof(LevelSlot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[gtid] = 0u;
+    uint32_t nf = 0;
+    unsigned long long mf = 0;
+    if (!bu) {
+      const uint32_t qc = __ldcg(&cur->qcount), cc = __ldcg(&cur->ccount);
+      td_level(a, L, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, fnext,
+               a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx, nf, mf);
+    } else {
+      bu_level(a, sh, L, fcur, fnext, nf, mf);
+    }
+    const unsigned long long bnf = block_sum_u64<kBlock>(nf);
+    const unsigned long long bmf = block_sum_u64<kBlock>(mf);
+    if (threadIdx.x == 0 && bnf) {
+      atomicAdd(&nx->nf, (uint32_t)bnf);
+      atomicAdd(&nx->mf, bmf);
+    }
+    if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+    const uint32_t NF = __ldcg(&nx->nf);
+    const unsigned long long MF = __ldcg(&nx->mf);
+    if (bu) ++bu_levels;
+    if (NF == 0) break;
+    nr += NF;
+    mr += MF;
+    mu = mu > MF ? mu - MF : 0;
+    bool nbu = bu;
+    if (!bu) {
+      if ((double)MF * a.alpha > (double)mu) nbu = true;
+    } else {
+      if ((double)NF * a.beta < (double)a.n && NF < prev_nf) nbu = false;
+    }
+    if (bu && !nbu) {
+      bitmap_to_queue(a, fnext, a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx);
+      if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+    }
+    if (nbu != bu) ++switches;
+    bu = nbu;
+    prev_nf = NF;
+    ++L;
+    if (L >= a.n + 1) {
+      if (gtid == 0) atomicOr(a.err, kErrLevels);
+      break;
+    }
+  }
+  // epilogue: unreached vertices read INFINIT
+  {
+    const uint32_t lane = lane_id();
+    const uint32_t gw = gtid >> 5, nw = nthreads >> 5;
+    for (uint32_t w = gw; w < a.W; w += nw) {
+      const uint32_t vis = __ldcg(a.visited + w);
+      const uint32_t v = w * 32 + lane;
+      if (!((vis >> lane) & 1u) && v < a.n) a.depth[v] = kInfinit;
+    }
+  }
+  if (gtid == 0) {
+    a.summary->levels = L + 1;
+    a.summary->bu_levels = bu_levels;
+    a.summary->switches = switches;
+    a.summary->nr = nr;
+    a.summary->mr = mr;
+  }
+}
+
+}  // namespace
+}  // namespace grus
+
+using namespace grus;
+
+extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
+                        grus_stats *stats, void *stream) {
+  if (!g || !depth) return GRUS_EINVAL;
+  if (g->n == 0 || src >= g->n) {
+    set_last_error("source vertex out of range");
+    return GRUS_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(g->mu);
+  Workspace *w = nullptr;
+  int rc = ws_get(g, &w);
+  if (rc) return rc;
+  const bool dev_out = is_device_pointer(depth);
+  if (!dev_out && !w->depth) GRUS_CUDA_TRY(cudaMalloc(&w->depth, g->n * 4));
+
+  static int occ = -1;
+  if (occ < 0) {
+    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bfs_persistent, kBlock, 0));
+  }
+  const int sms = device_sm_count();
+  int per_sm = occ;
+  if (g->tuning.ctas_per_sm) per_sm = std::min<int>(per_sm, (int)g->tuning.ctas_per_sm);
+  if (per_sm < 1) {
+    set_last_error("bfs kernel cannot be resident");
+    return GRUS_ECUDA;
+  }
+
+  Args a;
+  std::memset(&a, 0, sizeof(a));
+  a.offs = g->csr.offs;
+  a.cols = g->csr.cols;
+  a.n = (uint32_t)g->n;
+  a.W = w->W;
+  a.m = g->m;
+  a.src = src;
+  a.depth = dev_out ? depth : w->depth;
+  const uint64_t Wp = ((uint64_t)w->W + 31) / 32 * 32;
+  a.visited = w->bitmaps;
+  a.front[0] = w->bitmaps + Wp;
+  a.front[1] = w->bitmaps + 2 * Wp;
+  a.front[2] = w->bitmaps + 3 * Wp;
+  a.queue[0] = w->queues;
+  a.queue[1] = w->queues + g->n;
+  a.chunks[0] = w->chunks;
+  a.chunks[1] = w->chunks + w->chunk_cap;
+  a.queue_cap = (uint32_t)g->n;
+  a.chunk_cap = w->chunk_cap;
+  a.slots = (LevelSlot *)(w->ctrl + kOffSlots);
+  a.bar = (GridBarrier *)(w->ctrl + kOffBar);
+  a.err = (uint32_t *)(w->ctrl + kOffErr);
+  a.summary = (Summary *)(w->ctrl + kOffSummary);
+  a.alpha = tune_or(g->tuning.alpha, kDefAlpha);
+  a.beta = tune_or(g->tuning.beta, kDefBeta);
+  a.huge = tune_or(g->tuning.huge_degree, kDefHuge);
+  a.bu_scan = tune_or(g->tuning.bu_scan, kDefBuScan);
+  a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
+
+  cudaLaunchAttribute attrs[2];
+  int nattr = 0;
+  attrs[nattr].id = cudaLaunchAttributeCooperative;
+  attrs[nattr].val.cooperative = 1;
+  ++nattr;
+  const int win = l2_window(s, w->bitmaps, w->bitmap_bytes);
+  if (win > 0) {
+    attrs[nattr].id = cudaLaunchAttributeAccessPolicyWindow;
+    attrs[nattr].val.accessPolicyWindow.base_ptr = w->bitmaps;
+    attrs[nattr].val.accessPolicyWindow.num_bytes = (size_t)win;
+    attrs[nattr].val.accessPolicyWindow.hitRatio = 1.0f;
+    attrs[nattr].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attrs[nattr].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    ++nattr;
+  }
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)(sms * per_sm));
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cfg.attrs = attrs;
+  cfg.numAttrs = nattr;
+
+  const bool sync = stats != nullptr || !dev_out;
+  if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
+  GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, bfs_persistent, a));
+  if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev1, s));
+  if (!dev_out) GRUS_CUDA_TRY(cudaMemcpyAsync(depth, w->depth, g->n * 4, cudaMemcpyDeviceToHost, s));
+  if (!sync) return GRUS_OK;
+  GRUS_CUDA_TRY(cudaMemcpyAsync(w->ctrl_host, w->ctrl, kCtrlBytes, cudaMemcpyDeviceToHost, s));
+  GRUS_CUDA_TRY(cudaStreamSynchronize(s));
+  const uint32_t errbits = *(uint32_t *)(w->ctrl_host + kOffErr);
+  if (errbits) {
+    // reset the control block so the next call starts clean
+    cudaMemsetAsync(w->ctrl, 0, kCtrlBytes, s);
+    cudaStreamSynchronize(s);
+    return status_from_device_error(errbits);
+  }
+  if (stats) {
+    const Summary *sm = (const Summary *)(w->ctrl_host + kOffSummary);
+    std::memset(stats, 0, sizeof(*stats));
+    stats->levels = sm->levels;
+    stats->bottom_up_levels = sm->bu_levels;
+    stats->direction_switches = sm->switches;
+    stats->kernel_launches = 1;
+    stats->vertices_reached = sm->nr;
+    stats->edges_reached = sm->mr;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+    stats->device_ms = ms;
+  }
+  return GRUS_OK;
+}

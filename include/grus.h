@@ -1,0 +1,162 @@
+/*
+ * grus.h -- C ABI of libgrus, the GB300 (sm_103a) frontier-traversal core.
+ *
+ * The reference (Grus) exposes no C ABI: its path sits behind C++ templates
+ * (include/kernel.cuh, frontier.cuh, graph.cuh, graph_loader.cuh) and the
+ * samples' command lines.  Each entry point below names the reference
+ * interface whose job it takes over, so a maintainer can bind the path from
+ * C, ctypes or any FFI.  The mgg drop-in headers in
+ * grus_framework_gb300/mgg/ keep the template API itself.
+ *
+ * Conventions
+ *   - Every call returns an int status: 0 on success, a negative code below
+ *     on failure.  The library never calls exit() (unlike H_ERR,
+ *     include/common.cuh:57-68).  grus_last_error() gives a detail string.
+ *   - The library owns graph handles; the caller owns output buffers.  An
+ *     output pointer may be host memory (pinned or pageable) or device
+ *     memory; the call detects which and copies as needed.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy stream).
+ *     Calls with host outputs or a non-NULL stats pointer return after the
+ *     work has finished; calls with device outputs and no stats are
+ *     asynchronous on `stream`.
+ *   - Vertex ids and CSR arrays are uint32 (vtx_t, include/common.cuh:48);
+ *     unreached vertices read GRUS_INFINIT (INFINIT, include/common.cuh:52).
+ */
+#ifndef GRUS_H
+#define GRUS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define GRUS_OK 0
+#define GRUS_ENOENT (-2)
+#define GRUS_EIO (-5)
+#define GRUS_ENOMEM (-12)
+#define GRUS_EBUSY (-16)
+#define GRUS_ENODEV (-19)
+#define GRUS_EINVAL (-22)
+#define GRUS_EOVERFLOW (-75)
+#define GRUS_ETIMEDOUT (-110)
+#define GRUS_ECUDA (-1000)
+
+#define GRUS_INFINIT 4294967294u
+
+/* memory modes (include/graph.cuh:170-251 Set_Mem_Policy) */
+#define GRUS_MEM_DEVICE 0  /* CSR in HBM (cudaMalloc) */
+#define GRUS_MEM_MANAGED 1 /* CSR in managed memory, prefetched up to a budget */
+
+/* graph flags */
+#define GRUS_GRAPH_SYMMETRIC 1u /* every edge (u,v) has (v,u): CSR == CSC */
+#define GRUS_GRAPH_WEIGHTED 2u  /* uint32 edge weights present */
+
+/* generator flags */
+#define GRUS_GEN_SYMMETRIC 1u
+#define GRUS_GEN_WEIGHTED 2u
+#define GRUS_GEN_RELABEL 4u
+
+#if defined(__GNUC__)
+#define GRUS_API __attribute__((visibility("default")))
+#else
+#define GRUS_API
+#endif
+
+typedef struct grus_graph grus_graph;
+
+typedef struct grus_graph_info {
+  uint64_t n;                   /* numNode (include/graph.cuh:116) */
+  uint64_t m;                   /* numEdge (include/graph.cuh:117) */
+  uint32_t max_degree_vertex;   /* first vertex of maximum out-degree */
+  uint32_t max_degree;
+  uint32_t flags;               /* GRUS_GRAPH_* */
+  int32_t mem_mode;             /* GRUS_MEM_* */
+  const uint32_t *offsets;      /* xadj   (device-accessible, n+1) */
+  const uint32_t *cols;         /* adjncy (device-accessible, m)   */
+  const uint32_t *weights;      /* adjwgt (device-accessible, m) or NULL */
+  const uint32_t *t_offsets;    /* CSC arrays, NULL until built */
+  const uint32_t *t_cols;
+  const uint32_t *t_weights;
+  uint64_t budget_bytes;        /* managed mode device budget, else 0 */
+} grus_graph_info;
+
+typedef struct grus_stats {
+  uint32_t levels;              /* frontier iterations (job.itr at loop end) */
+  uint32_t bottom_up_levels;    /* iterations run in pull direction */
+  uint32_t direction_switches;
+  uint32_t kernel_launches;     /* device kernels launched by this call */
+  uint64_t vertices_reached;
+  uint64_t edges_reached;       /* m_r: sum of out-degree of reached vertices */
+  uint64_t edges_relaxed;       /* SSSP: edge relaxations performed */
+  float device_ms;              /* CUDA-event time of the device work */
+  uint32_t reserved0;
+} grus_stats;
+
+/* Autotunable launch/heuristic parameters (0 fields mean "default"). */
+typedef struct grus_tuning {
+  float alpha;            /* push->pull when m_f > m_u / alpha (Beamer) */
+  float beta;             /* pull->push when n_f < n / beta */
+  uint32_t ctas_per_sm;   /* persistent grid = SMs x ctas_per_sm (<= occupancy) */
+  uint32_t huge_degree;   /* degree at/above which a vertex is split into chunks */
+  uint32_t bu_scan;       /* neighbours a pull thread checks before deferring */
+  uint32_t timeout_ms;    /* bound on every device-side wait */
+} grus_tuning;
+
+/* ---- library ------------------------------------------------------------- */
+GRUS_API const char *grus_version(void);
+/* Text of a status code. */
+GRUS_API const char *grus_strerror(int status);
+/* Detail of the last failing call on this host thread. */
+GRUS_API const char *grus_last_error(void);
+/* Select and initialise a device (FLAGS_device, include/app.cuh:18). */
+GRUS_API int grus_device_init(int device);
+
+/* ---- graphs -------------------------------------------------------------- */
+/* CSR from host arrays.  Replaces graph_t<CSR> filled by
+ * graph_loader::ReadGraphGR (include/graph_loader.cuh:65-159). */
+GRUS_API int grus_graph_from_csr(uint64_t n, uint64_t m, const uint32_t *offsets,
+                        const uint32_t *cols, const uint32_t *weights,
+                        uint32_t flags, int mem_mode, uint64_t budget_bytes,
+                        grus_graph **out);
+/* Load a Galois v1 .gr file.  Replaces graph_loader::Load
+ * (include/graph_loader.cuh:160-166) + Set_Mem_Policy
+ * (include/graph.cuh:170-251).  need_weights mirrors Load's _needweight. */
+GRUS_API int grus_graph_load_gr(const char *path, int need_weights, int mem_mode,
+                       uint64_t budget_bytes, grus_graph **out);
+/* Write the graph as .gr (the layout graph_loader.cuh:65-159 reads). */
+GRUS_API int grus_graph_save_gr(const grus_graph *g, const char *path);
+/* Seeded RMAT (a,b,c,d = .57,.19,.19,.05) generated on the device; the
+ * reference has no generator (it reads Galois-converted files, README.md). */
+GRUS_API int grus_graph_rmat(int scale, int edge_factor, uint64_t seed,
+                    uint32_t gen_flags, int mem_mode, uint64_t budget_bytes,
+                    grus_graph **out);
+/* rows x cols 4-neighbour grid, vertex id r*cols+c. */
+GRUS_API int grus_graph_grid2d(uint32_t rows, uint32_t cols, uint64_t seed,
+                      uint32_t gen_flags, grus_graph **out);
+GRUS_API int grus_graph_get_info(const grus_graph *g, grus_graph_info *info);
+/* Copy CSR (and CSC when built) back to host arrays (any may be NULL). */
+GRUS_API int grus_graph_copy_csr(const grus_graph *g, uint32_t *offsets, uint32_t *cols,
+                        uint32_t *weights);
+/* Device transpose CSR->CSC with weights.  Replaces the host-serial
+ * csr_tocsc/CSR2CSC (include/graph.cuh:273-320), which drops weights. */
+GRUS_API int grus_graph_build_csc(grus_graph *g);
+GRUS_API int grus_graph_copy_csc(const grus_graph *g, uint32_t *t_offsets,
+                        uint32_t *t_cols, uint32_t *t_weights);
+GRUS_API int grus_graph_set_tuning(grus_graph *g, const grus_tuning *t);
+GRUS_API int grus_graph_get_tuning(const grus_graph *g, grus_tuning *t);
+GRUS_API int grus_graph_free(grus_graph *g);
+
+/* ---- traversals ----------------------------------------------------------- */
+/* Single-source BFS depths.  Replaces the BFS_single_gpu level loop
+ * (samples/bfs/bfs.cu:135-173) over kernel<...,Frontier<BDF>> / kernel_pull
+ * (include/kernel.cuh:124-165): one persistent direction-optimising launch. */
+GRUS_API int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth, grus_stats *stats,
+             void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRUS_H */

@@ -1,0 +1,129 @@
+"""GPU: device generator and BFS against the CPU oracle, through the C ABI.
+
+BFS depths are integer results and must match bit for bit (the fixpoint of
+samples/bfs/bfs.cu:18-87), on the golden fixtures, on RMAT-16 (the C1
+configuration), on directed and high-diameter graphs, and -- through the
+size-independent checks that the serial oracle can afford -- on RMAT-22.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+INF = 4294967294
+ANSWERS = json.loads((GOLDEN / "known_answers.json").read_text())
+
+
+def host_csr(g):
+    offs, cols, wts = g.copy_csr()
+    import oracle
+    return oracle.CSR(offs, cols, wts)
+
+
+@pytest.mark.parametrize("scale,ef,seed,flags", [
+    (8, 4, 3, 0), (10, 16, 1, 1 | 4), (12, 8, 2, 1 | 2 | 4), (11, 16, 3, 2 | 4), (14, 16, 1, 1 | 4),
+])
+def test_rmat_generator_matches_oracle(grus, oracle_mod, scale, ef, seed, flags):
+    g = grus.Graph.rmat(scale, ef, seed, symmetric=bool(flags & 1), weighted=bool(flags & 2),
+                        relabel=bool(flags & 4))
+    ref = oracle_mod.rmat(scale, ef, seed, flags)
+    offs, cols, wts = g.copy_csr()
+    assert np.array_equal(offs, ref.offs)
+    assert np.array_equal(cols, ref.cols)
+    if flags & 2:
+        assert np.array_equal(wts, ref.wts)
+    assert g.max_degree_vertex == oracle_mod.max_degree_vertex(ref)
+    g.free()
+
+
+def test_grid_generator_matches_oracle(grus, oracle_mod):
+    g = grus.Graph.grid2d(37, 53, seed=5, weighted=True)
+    ref = oracle_mod.grid(37, 53, 5, 2)
+    offs, cols, wts = g.copy_csr()
+    assert np.array_equal(offs, ref.offs) and np.array_equal(cols, ref.cols)
+    assert np.array_equal(wts, ref.wts)
+
+
+@pytest.mark.parametrize("name", sorted(ANSWERS))
+def test_bfs_golden_fixtures(grus, name):
+    a = ANSWERS[name]
+    g = grus.Graph.load_gr(GOLDEN / f"{name}.gr")
+    for s, exp in a["bfs"].items():
+        d, st = grus.bfs(g, int(s), stats=True)
+        assert d.tolist() == exp
+        assert st["vertices_reached"] == sum(x != INF for x in exp)
+    g.free()
+
+
+def _check_bfs(grus, oracle_mod, g, srcs):
+    h = host_csr(g)
+    for s in srcs:
+        d, st = grus.bfs(g, int(s), stats=True)
+        ref = oracle_mod.bfs(h, int(s))
+        assert np.array_equal(d, ref), f"src {s}: {np.count_nonzero(d != ref)} mismatches"
+        assert st["vertices_reached"] == int(np.count_nonzero(ref != INF))
+        assert st["edges_reached"] == oracle_mod.reached_edges(h, ref)
+        reached = ref[ref != INF]
+        assert st["levels"] == int(reached.max()) + 1
+    return h
+
+
+def test_bfs_rmat16_c1(grus, oracle_mod):
+    """C1: RMAT scale 16, ef 16, seed 1, symmetrised, source = max-degree vertex."""
+    g = grus.Graph.rmat(16, 16, 1, symmetric=True)
+    rng = np.random.default_rng(0)
+    _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, *rng.integers(0, g.n, 4)])
+
+
+@pytest.mark.parametrize("alpha,beta", [(15.0, 18.0), (1e9, 18.0), (1e-6, 1e9), (2.0, 2.0)])
+def test_bfs_direction_policies(grus, oracle_mod, alpha, beta):
+    """Push-only, pull-heavy and frequent-switch schedules all give the same depths."""
+    g = grus.Graph.rmat(15, 16, 7, symmetric=True)
+    g.set_tuning(alpha=alpha, beta=beta)
+    _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, 5, 12345])
+
+
+@pytest.mark.parametrize("huge,bu_scan,ctas", [(64, 4, 1), (1 << 20, 64, 2), (512, 1, 0)])
+def test_bfs_bins_and_launch_shapes(grus, oracle_mod, huge, bu_scan, ctas):
+    g = grus.Graph.rmat(14, 32, 9, symmetric=True)
+    g.set_tuning(huge_degree=huge, bu_scan=bu_scan, ctas_per_sm=ctas)
+    _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, 77])
+
+
+def test_bfs_directed_rmat(grus, oracle_mod):
+    g = grus.Graph.rmat(14, 16, 3, symmetric=False)
+    _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, 0, 999])
+
+
+def test_bfs_grid_high_diameter(grus, oracle_mod):
+    g = grus.Graph.grid2d(300, 200)
+    _check_bfs(grus, oracle_mod, g, [201, 0, 59999])
+
+
+def test_bfs_device_output_and_stream(grus, oracle_mod):
+    torch = pytest.importorskip("torch")
+    g = grus.Graph.rmat(13, 16, 5, symmetric=True)
+    out = torch.empty(g.n, dtype=torch.int32, device="cuda")
+    s = torch.cuda.Stream()
+    grus.bfs(g, g.max_degree_vertex, out=out, stream=s)
+    s.synchronize()
+    ref = oracle_mod.bfs(host_csr(g), g.max_degree_vertex)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), ref)
+
+
+def test_bfs_errors(grus):
+    g = grus.Graph.rmat(8, 4, 1)
+    with pytest.raises(grus.GrusError) as e:
+        grus.bfs(g, g.n)
+    assert e.value.status == grus.EINVAL
+    with pytest.raises(grus.GrusError):
+        grus.Graph.load_gr(GOLDEN / "does_not_exist.gr")
+
+
+@pytest.mark.slow
+def test_bfs_rmat22_full_size(grus, oracle_mod):
+    g = grus.Graph.rmat(22, 16, 2, symmetric=True)
+    _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex])
