@@ -1,9 +1,9 @@
 """grus_framework_gb300 -- GB300-native frontier-traversal core (Grus drop-in).
 
 Python host side over the C ABI in include/grus.h (libgrus.so, hand-written
-sm_103a CUDA).  There is no CPU fallback: importing the package loads the
-library and raises if it has not been built (``__graft_entry__.build()`` or
-``python -m grus_framework_gb300.build``).
+sm_103a CUDA).  There is no CPU fallback: the first call into the package
+loads the library and raises ImportError if it has not been built
+(``__graft_entry__.build()`` or ``python -m grus_framework_gb300.build``).
 
 The names follow the reference's interface: a graph is loaded from a Galois
 ``.gr`` file (graph_loader::Load, include/graph_loader.cuh:160-166) or built
@@ -69,6 +69,7 @@ class Tuning(C.Structure):
     _fields_ = [
         ("alpha", C.c_float), ("beta", C.c_float), ("ctas_per_sm", C.c_uint32),
         ("huge_degree", C.c_uint32), ("bu_scan", C.c_uint32), ("timeout_ms", C.c_uint32),
+        ("sssp_delta", C.c_uint32),
     ]
 
 
@@ -98,6 +99,9 @@ def _load():
         "grus_graph_get_tuning": ([vp, C.POINTER(Tuning)], i32),
         "grus_graph_free": ([vp], i32),
         "grus_bfs": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
+        "grus_sssp": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
+        "grus_cc": ([vp, vp, C.POINTER(Stats), vp], i32),
+        "grus_pagerank": ([vp, C.c_float, i32, vp, C.POINTER(Stats), vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -106,7 +110,18 @@ def _load():
     return L
 
 
-lib = _load()
+class _LazyLib:
+    """Loads libgrus.so on first use; raises ImportError if it is missing."""
+
+    _handle = None
+
+    def __getattr__(self, name):
+        if _LazyLib._handle is None:
+            _LazyLib._handle = _load()
+        return getattr(_LazyLib._handle, name)
+
+
+lib = _LazyLib()
 
 
 def _strerror(status):
@@ -301,4 +316,33 @@ def bfs(g: Graph, src: int, out=None, stream=None, stats: bool = False):
     st = Stats() if stats else None
     _check(lib.grus_bfs(g._handle(), src, _ptr(out), C.byref(st) if st is not None else None,
                         _stream(stream)), "grus_bfs")
+    return (out, st.as_dict()) if stats else out
+
+
+def sssp(g: Graph, src: int, out=None, stream=None, stats: bool = False):
+    """Exact shortest-path distances from `src` over the uint32 edge weights."""
+    out = _out_array(g, out, np.uint32)
+    st = Stats() if stats else None
+    _check(lib.grus_sssp(g._handle(), src, _ptr(out), C.byref(st) if st is not None else None,
+                         _stream(stream)), "grus_sssp")
+    return (out, st.as_dict()) if stats else out
+
+
+def cc(g: Graph, out=None, stream=None, stats: bool = False):
+    """Connected-component labels: the minimum vertex id of each component."""
+    out = _out_array(g, out, np.uint32)
+    st = Stats() if stats else None
+    _check(lib.grus_cc(g._handle(), _ptr(out), C.byref(st) if st is not None else None,
+                       _stream(stream)), "grus_cc")
+    return (out, st.as_dict()) if stats else out
+
+
+def pagerank(g: Graph, damping: float = 0.85, iters: int = 20, out=None, stream=None,
+             stats: bool = False):
+    """Pull PageRank (FP32 ranks, r0 = 1/n, no dangling redistribution)."""
+    out = _out_array(g, out, np.float32)
+    st = Stats() if stats else None
+    _check(lib.grus_pagerank(g._handle(), damping, iters, _ptr(out),
+                             C.byref(st) if st is not None else None, _stream(stream)),
+           "grus_pagerank")
     return (out, st.as_dict()) if stats else out

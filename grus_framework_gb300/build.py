@@ -32,6 +32,9 @@ SOURCES = [
     "graph.cu",
     "graph_gen.cu",
     "bfs.cu",
+    "sssp.cu",
+    "cc.cu",
+    "pagerank.cu",
 ]
 
 

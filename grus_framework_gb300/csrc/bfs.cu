@@ -28,6 +28,9 @@
 //     are deferred to a CTA list and finished warp-cooperatively (32
 //     neighbours per ballot).  The word's next-frontier and visited bits are
 //     written with one store per warp.
+//   * pull levels read in-edges: the CSR itself on a symmetric graph, the CSC
+//     (grus_graph_build_csc) on a directed one; without a CSC a directed graph
+//     runs push-only.
 //   * direction: Beamer's heuristic -- push->pull when m_f > m_u/alpha,
 //     pull->push when n_f < n/beta and the frontier shrinks; switching back to
 //     push compacts the frontier bitmap into the binned queue.
@@ -36,15 +39,13 @@
 #include <algorithm>
 #include <cstring>
 
-#include "grus_internal.cuh"
+#include "expand.cuh"
 
 namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
-constexpr uint32_t kChunk = 4096;     // edges per chunk work item
-constexpr uint32_t kCtaTh = 256;      // CTA-cooperative degree threshold
 constexpr uint32_t kDefHuge = 8192;   // chunking threshold
 constexpr uint32_t kDefBuScan = 8;    // pull: neighbours checked before deferring
 constexpr int kDeferCap = 1024;       // pull: deferred vertices per CTA
@@ -65,8 +66,11 @@ struct Summary {
 };
 
 struct Args {
-  const uint32_t *__restrict__ offs;
+  const uint32_t *__restrict__ offs;   // out-edges (push levels)
   const uint32_t *__restrict__ cols;
+  const uint32_t *__restrict__ ioffs;  // in-edges (pull levels): the CSR itself
+  const uint32_t *__restrict__ icols;  // on a symmetric graph, else the CSC
+  bool allow_pull;                     // false when no in-edge arrays exist
   uint32_t n, W;
   uint64_t m;
   uint32_t src;
@@ -151,143 +155,43 @@ int ws_get(grus_graph *g, Workspace **out) {
 }
 
 // ---------------------------------------------------------------------------
-// push-direction visit of one edge target
+// push level: visitor for expand_binned (expand.cuh)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void td_visit(const Args &a, uint32_t dst, uint32_t nd,
-                                         uint32_t *fnext, uint32_t *qnext,
-                                         uint4 *cnext, LevelSlot *nx,
-                                         uint32_t &nf, unsigned long long &mf) {
-  const uint32_t w = dst >> 5, bit = 1u << (dst & 31u);
-  if (__ldcg(a.visited + w) & bit) return;
-  if (atomicOr(a.visited + w, bit) & bit) return;
-  a.depth[dst] = nd;
-  atomicOr(fnext + w, bit);
-  const uint32_t b = __ldg(a.offs + dst), e = __ldg(a.offs + dst + 1);
-  const uint32_t d = e - b;
-  nf += 1;
-  mf += d;
-  if (d == 0) return;
-  if (d < a.huge) {
-    const uint32_t pos = agg_reserve(&nx->qcount);
-    if (pos < a.queue_cap) qnext[pos] = dst;
-    else atomicOr(a.err, kErrOverflow);
-  } else {
-    const uint32_t nch = (d + kChunk - 1) / kChunk;
-    const uint32_t pos = atomicAdd(&nx->ccount, nch);
-    if (pos + nch <= a.chunk_cap) {
-      for (uint32_t c = 0; c < nch; ++c)
-        cnext[pos + c] = make_uint4(dst, b + c * kChunk, min(e, b + (c + 1) * kChunk), 0u);
-    } else {
-      atomicOr(a.err, kErrOverflow);
-    }
-  }
-}
+struct PushVisitor {
+  const Args *a;
+  uint32_t nd;
+  uint32_t *fnext, *qnext;
+  uint4 *cnext;
+  LevelSlot *nx;
+  uint32_t nf;
+  unsigned long long mf;
 
-// Queue an already-claimed vertex (used when converting a bitmap frontier).
+  __device__ __forceinline__ uint32_t aux(uint32_t) const { return 0u; }
+  // Claim dst with one atomicOr on the visited bitmap; the winner writes the
+  // depth, marks the next frontier and appends dst to the binned lists.
+  __device__ __forceinline__ void edge(uint32_t, uint32_t, uint32_t x) {
+    const uint32_t dst = __ldg(a->cols + x);
+    const uint32_t w = dst >> 5, bit = 1u << (dst & 31u);
+    if (__ldcg(a->visited + w) & bit) return;
+    if (atomicOr(a->visited + w, bit) & bit) return;
+    a->depth[dst] = nd;
+    atomicOr(fnext + w, bit);
+    const uint32_t b = __ldg(a->offs + dst), e = __ldg(a->offs + dst + 1);
+    nf += 1;
+    mf += e - b;
+    if (!push_binned(dst, b, e, a->huge, qnext, &nx->qcount, a->queue_cap, cnext,
+                     &nx->ccount, a->chunk_cap))
+      atomicOr(a->err, kErrOverflow);
+  }
+};
+
 __device__ __forceinline__ void enqueue_binned(const Args &a, uint32_t v,
                                                uint32_t *qnext, uint4 *cnext,
                                                LevelSlot *nx) {
   const uint32_t b = __ldg(a.offs + v), e = __ldg(a.offs + v + 1);
-  const uint32_t d = e - b;
-  if (d == 0) return;
-  if (d < a.huge) {
-    const uint32_t pos = agg_reserve(&nx->qcount);
-    if (pos < a.queue_cap) qnext[pos] = v;
-    else atomicOr(a.err, kErrOverflow);
-  } else {
-    const uint32_t nch = (d + kChunk - 1) / kChunk;
-    const uint32_t pos = atomicAdd(&nx->ccount, nch);
-    if (pos + nch <= a.chunk_cap) {
-      for (uint32_t c = 0; c < nch; ++c)
-        cnext[pos + c] = make_uint4(v, b + c * kChunk, min(e, b + (c + 1) * kChunk), 0u);
-    } else {
-      atomicOr(a.err, kErrOverflow);
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// push level: binned expansion of the queue and chunk list of level L
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void td_level(const Args &a, uint32_t L,
-                                         const uint32_t *qcur, uint32_t qcount,
-                                         const uint4 *ccur, uint32_t ccount,
-                                         uint32_t *fnext, uint32_t *qnext,
-                                         uint4 *cnext, LevelSlot *nx,
-                                         uint32_t &nf, unsigned long long &mf) {
-  __shared__ uint32_t s_owner, s_beg, s_end;
-  const uint32_t nd = L + 1;
-  const uint32_t lane = lane_id();
-  for (uint32_t base = blockIdx.x * kBlock; base < qcount; base += gridDim.x * kBlock) {
-    const uint32_t i = base + threadIdx.x;
-    uint32_t beg = 0, end = 0;
-    if (i < qcount) {
-      const uint32_t v = __ldcg(qcur + i);
-      beg = __ldg(a.offs + v);
-      end = __ldg(a.offs + v + 1);
-    }
-    // CTA-cooperative: one vertex at a time, whole block strides its list
-    while (true) {
-      if (threadIdx.x == 0) s_owner = 0xFFFFFFFFu;
-      __syncthreads();
-      if (end - beg >= kCtaTh) s_owner = threadIdx.x;
-      __syncthreads();
-      const uint32_t owner = s_owner;
-      if (owner == 0xFFFFFFFFu) break;
-      if (threadIdx.x == owner) {
-        s_beg = beg;
-        s_end = end;
-        beg = end;
-      }
-      __syncthreads();
-      const uint32_t cb = s_beg, ce = s_end;
-      for (uint32_t x = cb + threadIdx.x; x < ce; x += kBlock)
-        td_visit(a, __ldg(a.cols + x), nd, fnext, qnext, cnext, nx, nf, mf);
-      __syncthreads();
-    }
-    // warp-cooperative
-    while (true) {
-      const uint32_t ball = __ballot_sync(0xffffffffu, end - beg >= 32);
-      if (!ball) break;
-      const int leader = __ffs(ball) - 1;
-      const uint32_t wb = __shfl_sync(0xffffffffu, beg, leader);
-      const uint32_t we = __shfl_sync(0xffffffffu, end, leader);
-      if ((int)lane == leader) beg = end;
-      for (uint32_t x = wb + lane; x < we; x += 32)
-        td_visit(a, __ldg(a.cols + x), nd, fnext, qnext, cnext, nx, nf, mf);
-    }
-    // scan-based gather over the warp's remaining short lists
-    const uint32_t deg = end - beg;
-    uint32_t incl = deg;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-      if ((int)lane >= o) incl += t;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    for (uint32_t k0 = 0; k0 < total; k0 += 32) {
-      const uint32_t k = k0 + lane;
-      int j = 0;
-#pragma unroll
-      for (int step = 16; step >= 1; step >>= 1) {
-        const uint32_t pv = __shfl_sync(0xffffffffu, incl, j + step - 1);
-        if (pv <= k) j += step;
-      }
-      const uint32_t ob = __shfl_sync(0xffffffffu, beg, j);
-      const uint32_t oi = __shfl_sync(0xffffffffu, incl, j);
-      const uint32_t od = __shfl_sync(0xffffffffu, deg, j);
-      if (k < total) {
-        const uint32_t x = ob + (k - (oi - od));
-        td_visit(a, __ldg(a.cols + x), nd, fnext, qnext, cnext, nx, nf, mf);
-      }
-    }
-  }
-  // chunks of huge vertices: one CTA per 4096-edge chunk
-  for (uint32_t c = blockIdx.x; c < ccount; c += gridDim.x) {
-    const uint4 ch = __ldcg(ccur + c);
-    for (uint32_t x = ch.y + threadIdx.x; x < ch.z; x += kBlock)
-      td_visit(a, __ldg(a.cols + x), nd, fnext, qnext, cnext, nx, nf, mf);
-  }
+  if (!push_binned(v, b, e, a.huge, qnext, &nx->qcount, a.queue_cap, cnext, &nx->ccount,
+                   a.chunk_cap))
+    atomicOr(a.err, kErrOverflow);
 }
 
 // ---------------------------------------------------------------------------
@@ -308,7 +212,7 @@ __device__ __forceinline__ void bu_drain(const Args &a, PullShared &sh, uint32_t
     bool hit = false;
     for (uint32_t base = d.y; base < d.z; base += 32) {
       const uint32_t x = base + lane;
-      const bool h = x < d.z && test_bit(fcur, __ldg(a.cols + x));
+      const bool h = x < d.z && test_bit(fcur, __ldg(a.icols + x));
       if (__ballot_sync(0xffffffffu, h)) {
         hit = true;
         break;
@@ -320,7 +224,7 @@ __device__ __forceinline__ void bu_drain(const Args &a, PullShared &sh, uint32_t
       atomicOr(a.visited + (v >> 5), bit);
       atomicOr(fnext + (v >> 5), bit);
       nf += 1;
-      mf += d.z - d.w;
+      mf += __ldg(a.offs + v + 1) - __ldg(a.offs + v);
     }
   }
   __syncthreads();
@@ -344,16 +248,16 @@ __device__ __forceinline__ void bu_level(const Args &a, PullShared &sh, uint32_t
         bool found = false;
         uint32_t b = 0, e = 0;
         if (active) {
-          b = __ldg(a.offs + v);
-          e = __ldg(a.offs + v + 1);
+          b = __ldg(a.ioffs + v);
+          e = __ldg(a.ioffs + v + 1);
           const uint32_t lim = min(e, b + scan);
           uint32_t x = b;
           for (; x < lim; x += 4) {
             // four independent loads in flight, then four bitmap probes
-            uint32_t u0 = __ldg(a.cols + x);
-            uint32_t u1 = x + 1 < lim ? __ldg(a.cols + x + 1) : u0;
-            uint32_t u2 = x + 2 < lim ? __ldg(a.cols + x + 2) : u0;
-            uint32_t u3 = x + 3 < lim ? __ldg(a.cols + x + 3) : u0;
+            uint32_t u0 = __ldg(a.icols + x);
+            uint32_t u1 = x + 1 < lim ? __ldg(a.icols + x + 1) : u0;
+            uint32_t u2 = x + 2 < lim ? __ldg(a.icols + x + 2) : u0;
+            uint32_t u3 = x + 3 < lim ? __ldg(a.icols + x + 3) : u0;
             if (test_bit(fcur, u0) | test_bit(fcur, u1) | test_bit(fcur, u2) |
                 test_bit(fcur, u3)) {
               found = true;
@@ -366,7 +270,7 @@ __device__ __forceinline__ void bu_level(const Args &a, PullShared &sh, uint32_t
               sh.def[pos] = make_uint4(v, lim, e, b);
             } else {
               for (x = lim; x < e; ++x)
-                if (test_bit(fcur, __ldg(a.cols + x))) {
+                if (test_bit(fcur, __ldg(a.icols + x))) {
                   found = true;
                   break;
                 }
@@ -382,7 +286,7 @@ __device__ __forceinline__ void bu_level(const Args &a, PullShared &sh, uint32_t
           if (found) {
             a.depth[v] = nd;
             nf += 1;
-            mf += e - b;
+            mf += __ldg(a.offs + v + 1) - __ldg(a.offs + v);
           }
         }
       }
@@ -447,8 +351,10 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     unsigned long long mf = 0;
     if (!bu) {
       const uint32_t qc = __ldcg(&cur->qcount), cc = __ldcg(&cur->ccount);
-      td_level(a, L, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, fnext,
-               a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx, nf, mf);
+      PushVisitor vis{&a, L + 1, fnext, a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx, 0u, 0ull};
+      expand_binned<kBlock>(a.offs, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, vis);
+      nf = vis.nf;
+      mf = vis.mf;
     } else {
       bu_level(a, sh, L, fcur, fnext, nf, mf);
     }
@@ -468,7 +374,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     mu = mu > MF ? mu - MF : 0;
     bool nbu = bu;
     if (!bu) {
-      if ((double)MF * a.alpha > (double)mu) nbu = true;
+      if (a.allow_pull && (double)MF * a.alpha > (double)mu) nbu = true;
     } else {
       if ((double)NF * a.beta < (double)a.n && NF < prev_nf) nbu = false;
     }
@@ -540,6 +446,14 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   std::memset(&a, 0, sizeof(a));
   a.offs = g->csr.offs;
   a.cols = g->csr.cols;
+  // pull levels need in-edges: the CSR of a symmetric graph, else a built CSC
+  a.ioffs = g->csc.offs;
+  a.icols = g->csc.cols;
+  if (g->flags & GRUS_GRAPH_SYMMETRIC) {
+    a.ioffs = g->csr.offs;
+    a.icols = g->csr.cols;
+  }
+  a.allow_pull = a.ioffs != nullptr;
   a.n = (uint32_t)g->n;
   a.W = w->W;
   a.m = g->m;

@@ -658,3 +658,44 @@ int grus_graph_copy_csc(const grus_graph *g, uint32_t *t_offsets,
 }
 
 }  // extern "C"
+
+namespace grus {
+
+// Cooperative launch of a persistent kernel: SMs x min(occupancy, requested)
+// CTAs, with an L2 persisting access-policy window over [win_base, +win_bytes)
+// attached to this launch only (the caller's stream is left untouched).
+int launch_persistent(const void *fn, void **args, int block, int per_sm_req,
+                      int occupancy, cudaStream_t s, void *win_base, size_t win_bytes) {
+  int per_sm = occupancy;
+  if (per_sm_req > 0) per_sm = std::min(per_sm, per_sm_req);
+  if (per_sm < 1) {
+    set_last_error("persistent kernel cannot be resident");
+    return GRUS_ECUDA;
+  }
+  cudaLaunchAttribute attrs[2];
+  int nattr = 0;
+  attrs[nattr].id = cudaLaunchAttributeCooperative;
+  attrs[nattr].val.cooperative = 1;
+  ++nattr;
+  const int win = win_base ? l2_window(s, win_base, win_bytes) : 0;
+  if (win > 0) {
+    attrs[nattr].id = cudaLaunchAttributeAccessPolicyWindow;
+    attrs[nattr].val.accessPolicyWindow.base_ptr = win_base;
+    attrs[nattr].val.accessPolicyWindow.num_bytes = (size_t)win;
+    attrs[nattr].val.accessPolicyWindow.hitRatio = 1.0f;
+    attrs[nattr].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attrs[nattr].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    ++nattr;
+  }
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)(device_sm_count() * per_sm));
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.stream = s;
+  cfg.attrs = attrs;
+  cfg.numAttrs = nattr;
+  GRUS_CUDA_TRY(cudaLaunchKernelExC(&cfg, fn, args));
+  return GRUS_OK;
+}
+
+}  // namespace grus

@@ -1,0 +1,291 @@
+// pagerank.cu -- pull PageRank, FP32 ranks, fixed iteration count, one
+// persistent launch.
+//
+//   r_0(v) = 1/n,  r_{t+1}(v) = (1-d)/n + d * sum_{u -> v} r_t(u) / outdeg(u)
+//
+// Dangling mass is not redistributed, as in the reference, which never pushes
+// from out-degree-0 vertices (samples/pagerank/pr.cu:29-31,83).  The reference
+// itself runs a delta-push variant (pr.cu:17-90) whose pull mode is broken
+// (kernel_pull never calls job.prepare(), include/kernel.cuh:128-133); the
+// drop-in headers keep that sample's semantics, this entry point computes the
+// definition above.
+//
+// Layout: in-edges (CSC) from grus_graph_build_csc; a contribution array
+// c(u) = r(u)/outdeg(u) double-buffered across iterations, so an iteration is
+// one fused pass: gather c over in-edges, form r, write c_next (and r on the
+// last iteration).  Per 256-vertex tile, in-degree is binned:
+//   >= kCtaTh (1024) : whole CTA strides the list, block reduction
+//   >= 32            : one warp, shuffle reduction
+//   <  32            : one thread, loads unrolled four wide
+// Per-thread partial sums over more than kKahanTh terms use compensated
+// (Kahan-Babuska) summation; reductions across lanes are pairwise trees.
+// The contribution arrays sit in an L2 persisting window.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "grus_internal.cuh"
+
+namespace grus {
+
+int build_csc_locked(grus_graph *g);
+int launch_persistent(const void *fn, void **args, int block, int per_sm_req,
+                      int occupancy, cudaStream_t s, void *win_base, size_t win_bytes);
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr uint32_t kCtaTh = 1024;
+constexpr uint32_t kKahanTh = 16;
+
+struct Args {
+  const uint32_t *__restrict__ toffs;  // CSC offsets
+  const uint32_t *__restrict__ tcols;  // CSC sources
+  const uint32_t *__restrict__ offs;   // CSR offsets (out-degrees)
+  uint32_t n;
+  float base, damping;
+  int iters;
+  float *c[2];
+  float *rank;
+  GridBarrier *bar;
+  uint32_t *err;
+  uint64_t timeout_ns;
+};
+
+// Compensated accumulator (Neumaier's variant of Kahan summation).
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x;
+    c += fabsf(s) >= fabsf(x) ? (s - t) + x : (x - t) + s;
+    s = t;
+  }
+  __device__ __forceinline__ float value() const { return s + c; }
+};
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ float outdeg_inv(const Args &a, uint32_t v) {
+  const uint32_t d = __ldg(a.offs + v + 1) - __ldg(a.offs + v);
+  return d ? 1.0f / (float)d : 0.0f;
+}
+
+__device__ __forceinline__ void finish(const Args &a, uint32_t v, float sum, float *cn, bool last) {
+  const float r = a.base + a.damping * sum;
+  cn[v] = r * outdeg_inv(a, v);
+  if (last) a.rank[v] = r;
+}
+
+__device__ __forceinline__ float gather_seq(const Args &a, const float *cs, uint32_t b,
+                                            uint32_t e, uint32_t step) {
+  if (b >= e) return 0.f;
+  if ((e - b) <= kKahanTh * step) {
+    float s = 0.f;
+    for (uint32_t x = b; x < e; x += step) s += __ldcg(cs + __ldg(a.tcols + x));
+    return s;
+  }
+  KSum k;
+  for (uint32_t x = b; x < e; x += step) k.add(__ldcg(cs + __ldg(a.tcols + x)));
+  return k.value();
+}
+
+__global__ void __launch_bounds__(kBlock) pr_persistent(Args a) {
+  __shared__ uint32_t s_owner, s_v, s_beg, s_end;
+  __shared__ float s_part[kBlock / 32];
+  const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
+  const uint32_t nthreads = gridDim.x * kBlock;
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  const float r0 = 1.0f / (float)a.n;
+  for (uint32_t v = gtid; v < a.n; v += nthreads) a.c[0][v] = r0 * outdeg_inv(a, v);
+  if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+
+  for (int it = 0; it < a.iters; ++it) {
+    const float *cs = a.c[it & 1];
+    float *cn = a.c[(it + 1) & 1];
+    const bool last = it + 1 == a.iters;
+    for (uint32_t base = blockIdx.x * kBlock; base < a.n; base += gridDim.x * kBlock) {
+      const uint32_t v = base + threadIdx.x;
+      uint32_t beg = 0, end = 0;
+      if (v < a.n) {
+        beg = __ldg(a.toffs + v);
+        end = __ldg(a.toffs + v + 1);
+      }
+      bool done = v >= a.n;
+      // CTA-cooperative for very high in-degree
+      while (true) {
+        if (threadIdx.x == 0) s_owner = 0xFFFFFFFFu;
+        __syncthreads();
+        if (!done && end - beg >= kCtaTh) s_owner = threadIdx.x;
+        __syncthreads();
+        const uint32_t owner = s_owner;
+        if (owner == 0xFFFFFFFFu) break;
+        if (threadIdx.x == owner) {
+          s_v = v;
+          s_beg = beg;
+          s_end = end;
+          done = true;
+        }
+        __syncthreads();
+        const uint32_t cv = s_v, cb = s_beg, ce = s_end;
+        float part = warp_sum(gather_seq(a, cs, cb + threadIdx.x, ce, kBlock));
+        if (lane == 0) s_part[warp] = part;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          float tot = 0.f;
+          for (int i = 0; i < kBlock / 32; ++i) tot += s_part[i];
+          finish(a, cv, tot, cn, last);
+        }
+        __syncthreads();
+      }
+      // warp-cooperative
+      while (true) {
+        const uint32_t ball = __ballot_sync(0xffffffffu, !done && end - beg >= 32);
+        if (!ball) break;
+        const int leader = __ffs(ball) - 1;
+        const uint32_t wv = __shfl_sync(0xffffffffu, v, leader);
+        const uint32_t wb = __shfl_sync(0xffffffffu, beg, leader);
+        const uint32_t we = __shfl_sync(0xffffffffu, end, leader);
+        if ((int)lane == leader) done = true;
+        const float tot = warp_sum(gather_seq(a, cs, wb + lane, we, 32));
+        if ((int)lane == leader) finish(a, wv, tot, cn, last);
+      }
+      // one thread per short list, loads four wide
+      if (!done) {
+        float s = 0.f;
+        uint32_t x = beg;
+        for (; x + 4 <= end; x += 4) {
+          const uint32_t u0 = __ldg(a.tcols + x), u1 = __ldg(a.tcols + x + 1);
+          const uint32_t u2 = __ldg(a.tcols + x + 2), u3 = __ldg(a.tcols + x + 3);
+          const float f0 = __ldcg(cs + u0), f1 = __ldcg(cs + u1);
+          const float f2 = __ldcg(cs + u2), f3 = __ldcg(cs + u3);
+          s += (f0 + f1) + (f2 + f3);
+        }
+        for (; x < end; ++x) s += __ldcg(cs + __ldg(a.tcols + x));
+        finish(a, v, s, cn, last);
+      }
+    }
+    if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+  }
+}
+
+struct Workspace {
+  float *c = nullptr;   // 2 * n contributions
+  float *rank = nullptr;
+  char *ctrl = nullptr, *ctrl_host = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+constexpr size_t kOffBar = 0, kOffErr = 64, kCtrlBytes = 128;
+
+void ws_free(void *p) {
+  Workspace *w = (Workspace *)p;
+  if (!w) return;
+  cudaFree(w->c);
+  cudaFree(w->rank);
+  cudaFree(w->ctrl);
+  if (w->ctrl_host) cudaFreeHost(w->ctrl_host);
+  if (w->ev0) cudaEventDestroy(w->ev0);
+  if (w->ev1) cudaEventDestroy(w->ev1);
+  delete w;
+}
+
+int ws_get(grus_graph *g, Workspace **out) {
+  if (g->ws[kWsPr]) {
+    *out = (Workspace *)g->ws[kWsPr];
+    return GRUS_OK;
+  }
+  Workspace *w = new Workspace();
+  const uint64_t n1 = std::max<uint64_t>(g->n, 1);
+  cudaError_t e = cudaMalloc(&w->c, 2 * n1 * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaMemset(w->ctrl, 0, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaMallocHost(&w->ctrl_host, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaEventCreate(&w->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&w->ev1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ws_free(w);
+    set_last_error(std::string("pagerank workspace: ") + cudaGetErrorString(e));
+    return status_from_cuda(e);
+  }
+  g->ws[kWsPr] = w;
+  g->ws_free[kWsPr] = ws_free;
+  *out = w;
+  return GRUS_OK;
+}
+
+}  // namespace
+}  // namespace grus
+
+using namespace grus;
+
+extern "C" int grus_pagerank(grus_graph *g, float damping, int iters, float *rank,
+                             grus_stats *stats, void *stream) {
+  if (!g || !rank || iters < 0 || !(damping >= 0.f && damping <= 1.f)) return GRUS_EINVAL;
+  if (g->n == 0) return GRUS_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(g->mu);
+  int rc = build_csc_locked(g);
+  if (rc) return rc;
+  Workspace *w = nullptr;
+  rc = ws_get(g, &w);
+  if (rc) return rc;
+  const bool dev_out = is_device_pointer(rank);
+  if (!dev_out && !w->rank) GRUS_CUDA_TRY(cudaMalloc(&w->rank, g->n * 4));
+  static int occ = -1;
+  if (occ < 0)
+    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pr_persistent, kBlock, 0));
+  Args a;
+  std::memset(&a, 0, sizeof(a));
+  a.toffs = g->csc.offs;
+  a.tcols = g->csc.cols;
+  a.offs = g->csr.offs;
+  a.n = (uint32_t)g->n;
+  a.base = (1.0f - damping) / (float)g->n;
+  a.damping = damping;
+  a.iters = iters;
+  a.c[0] = w->c;
+  a.c[1] = w->c + g->n;
+  a.rank = dev_out ? rank : w->rank;
+  a.bar = (GridBarrier *)(w->ctrl + kOffBar);
+  a.err = (uint32_t *)(w->ctrl + kOffErr);
+  a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
+  if (iters == 0) {
+    // r_0 = 1/n
+    std::vector<float> h(g->n, 1.0f / (float)g->n);
+    GRUS_CUDA_TRY(cudaMemcpyAsync(rank, h.data(), g->n * 4, cudaMemcpyDefault, s));
+    GRUS_CUDA_TRY(cudaStreamSynchronize(s));
+    return GRUS_OK;
+  }
+  if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
+  void *args[] = {&a};
+  rc = launch_persistent((const void *)pr_persistent, args, kBlock, (int)g->tuning.ctas_per_sm,
+                         occ, s, w->c, 2 * g->n * 4);
+  if (rc) return rc;
+  if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev1, s));
+  if (!dev_out) GRUS_CUDA_TRY(cudaMemcpyAsync(rank, w->rank, g->n * 4, cudaMemcpyDeviceToHost, s));
+  if (!stats && dev_out) return GRUS_OK;
+  GRUS_CUDA_TRY(cudaMemcpyAsync(w->ctrl_host, w->ctrl, kCtrlBytes, cudaMemcpyDeviceToHost, s));
+  GRUS_CUDA_TRY(cudaStreamSynchronize(s));
+  const uint32_t errbits = *(uint32_t *)(w->ctrl_host + kOffErr);
+  if (errbits) {
+    cudaMemsetAsync(w->ctrl, 0, kCtrlBytes, s);
+    cudaStreamSynchronize(s);
+    return status_from_device_error(errbits);
+  }
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->levels = (uint32_t)iters;
+    stats->kernel_launches = 1;
+    stats->vertices_reached = g->n;
+    stats->edges_reached = g->m * (uint64_t)iters;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+    stats->device_ms = ms;
+  }
+  return GRUS_OK;
+}

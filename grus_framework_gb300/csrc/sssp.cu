@@ -1,0 +1,376 @@
+// sssp.cu -- exact single-source shortest paths over uint32 weights as one
+// persistent launch (near/far label correcting, a Delta-stepping variant:
+// Meyer & Sanders 2003; GPU near-far piles: Davidson et al. 2014).
+//
+// Replaces the reference's SSSP_single_gpu loop (samples/sssp/sssp.cu:123-170)
+// over kernel<...,Frontier<BDF>> whose updater relaxes with a NON-atomic
+// read-modify-write (sssp.cu:51-60) and can keep a larger distance when two
+// sources race.  Here every relaxation is atomicMin, so the result is the
+// unique fixpoint -- Dijkstra's distances -- whatever the schedule.
+//
+// Per iteration the near frontier (vertices whose distance improved and is
+// below the threshold T) is expanded with the degree-binned mappings of
+// expand.cuh.  An improved vertex v goes
+//   * to the next near frontier if dist(v) < T (deduplicated by a rotating
+//     bitmap), else
+//   * to the far pile (deduplicated by a far bitmap).
+// When the near frontier empties, T advances by Delta and the far pile is
+// split: entries below the old T were already expanded and are dropped,
+// entries below the new T become the near frontier, the rest stay.  If a
+// split yields nothing, T jumps to the bucket of the smallest far distance.
+// Every wait is a bounded grid barrier (grus_internal.cuh).
+#include <algorithm>
+#include <cstring>
+
+#include "expand.cuh"
+
+namespace grus {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr uint32_t kDefHuge = 8192;
+constexpr uint32_t kDefDelta = 96;
+
+struct Slot {
+  uint32_t qcount, ccount;
+  unsigned long long visits;  // edge relaxations attempted in the level
+  uint32_t pad[4];
+};
+
+// Far-pile control.  minfar is double-buffered by split parity so that the
+// value every CTA reads at the start of split k (written during split k-1) is
+// never the one being reset or reduced during split k.
+struct FarCtl {
+  uint32_t count[2];
+  uint32_t minfar[2];
+};
+
+struct Summary {
+  uint32_t levels, splits, pad0, pad1;
+  unsigned long long visits, nr, mr;
+};
+
+struct Args {
+  const uint32_t *__restrict__ offs;
+  const uint32_t *__restrict__ cols;
+  const uint32_t *__restrict__ wts;
+  uint32_t n, W;
+  uint32_t src;
+  uint32_t *dist;
+  uint32_t *inq[3];
+  uint32_t *farbm;
+  uint32_t *queue[2];
+  uint4 *chunks[2];
+  uint32_t *far[2];
+  uint32_t queue_cap, chunk_cap;
+  Slot *slots;
+  FarCtl *farctl;
+  GridBarrier *bar;
+  uint32_t *err;
+  Summary *summary;
+  uint32_t delta, huge;
+  uint64_t timeout_ns;
+};
+
+struct Workspace {
+  uint32_t W = 0;
+  uint32_t *dist = nullptr;
+  uint32_t *bitmaps = nullptr;  // 4 * Wp words: inq[3], farbm
+  size_t bitmap_bytes = 0;
+  uint32_t *queues = nullptr;   // 2n
+  uint32_t *far = nullptr;      // 2n
+  uint4 *chunks = nullptr;
+  uint32_t chunk_cap = 0;
+  char *ctrl = nullptr, *ctrl_host = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+constexpr size_t kOffSlots = 0, kOffFar = 256, kOffBar = 320, kOffErr = 384,
+                 kOffSummary = 448, kCtrlBytes = 512;
+
+void ws_free(void *p) {
+  Workspace *w = (Workspace *)p;
+  if (!w) return;
+  cudaFree(w->dist);
+  cudaFree(w->bitmaps);
+  cudaFree(w->queues);
+  cudaFree(w->far);
+  cudaFree(w->chunks);
+  cudaFree(w->ctrl);
+  if (w->ctrl_host) cudaFreeHost(w->ctrl_host);
+  if (w->ev0) cudaEventDestroy(w->ev0);
+  if (w->ev1) cudaEventDestroy(w->ev1);
+  delete w;
+}
+
+int ws_get(grus_graph *g, Workspace **out) {
+  if (g->ws[kWsSssp]) {
+    *out = (Workspace *)g->ws[kWsSssp];
+    return GRUS_OK;
+  }
+  Workspace *w = new Workspace();
+  w->W = (uint32_t)((g->n + 31) / 32);
+  const uint64_t Wp = ((uint64_t)w->W + 31) / 32 * 32;
+  w->bitmap_bytes = 4 * Wp * 4;
+  const uint32_t huge = tune_or(g->tuning.huge_degree, kDefHuge);
+  w->chunk_cap = (uint32_t)std::min<uint64_t>(g->m / kChunk + g->m / huge + 2, 0x7FFFFFFFull);
+  const uint64_t n1 = std::max<uint64_t>(g->n, 1);
+  cudaError_t e = cudaMalloc(&w->bitmaps, w->bitmap_bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&w->queues, 2 * n1 * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&w->far, 2 * n1 * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&w->chunks, 2ull * w->chunk_cap * sizeof(uint4));
+  if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaMemset(w->ctrl, 0, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaMallocHost(&w->ctrl_host, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaEventCreate(&w->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&w->ev1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ws_free(w);
+    set_last_error(std::string("sssp workspace: ") + cudaGetErrorString(e));
+    return status_from_cuda(e);
+  }
+  g->ws[kWsSssp] = w;
+  g->ws_free[kWsSssp] = ws_free;
+  *out = w;
+  return GRUS_OK;
+}
+
+// Marks v for the next near frontier (once per level) and queues it.
+__device__ __forceinline__ void to_near(const Args &a, uint32_t v, uint32_t *inq_next,
+                                        uint32_t *qnext, uint4 *cnext, Slot *nx) {
+  const uint32_t w = v >> 5, bit = 1u << (v & 31u);
+  if (__ldcg(inq_next + w) & bit) return;
+  if (atomicOr(inq_next + w, bit) & bit) return;
+  const uint32_t b = __ldg(a.offs + v), e = __ldg(a.offs + v + 1);
+  if (!push_binned(v, b, e, a.huge, qnext, &nx->qcount, a.queue_cap, cnext, &nx->ccount,
+                   a.chunk_cap))
+    atomicOr(a.err, kErrOverflow);
+}
+
+struct RelaxVisitor {
+  const Args *a;
+  uint32_t T;
+  uint32_t *inq_next, *qnext, *farp;
+  uint32_t *farcount;
+  uint4 *cnext;
+  Slot *nx;
+  unsigned long long visits;
+
+  __device__ __forceinline__ uint32_t aux(uint32_t v) const { return __ldcg(a->dist + v); }
+  __device__ __forceinline__ void edge(uint32_t, uint32_t du, uint32_t x) {
+    ++visits;
+    const uint32_t v = __ldg(a->cols + x);
+    const uint32_t nd = du + __ldg(a->wts + x);
+    if (nd >= __ldcg(a->dist + v)) return;
+    if (atomicMin(a->dist + v, nd) <= nd) return;
+    if (nd < T) {
+      to_near(*a, v, inq_next, qnext, cnext, nx);
+    } else {
+      const uint32_t w = v >> 5, bit = 1u << (v & 31u);
+      if (__ldcg(a->farbm + w) & bit) return;
+      if (atomicOr(a->farbm + w, bit) & bit) return;
+      const uint32_t pos = agg_reserve(farcount);
+      if (pos < a->queue_cap) farp[pos] = v;
+      else atomicOr(a->err, kErrOverflow);
+    }
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
+  const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
+  const uint32_t nthreads = gridDim.x * kBlock;
+  // prologue: distances to INFINIT, bitmaps and control words to zero
+  for (uint32_t i = gtid; i < a.n; i += nthreads) a.dist[i] = kInfinit;
+  {
+    const uint32_t words = (uint32_t)(a.farbm - a.inq[0]) + a.W;
+    for (uint32_t i = gtid; i < words; i += nthreads) a.inq[0][i] = 0u;
+    if (gtid < 4 * sizeof(Slot) / 4) ((uint32_t *)a.slots)[gtid] = 0u;
+    if (gtid < sizeof(FarCtl) / 4) ((uint32_t *)a.farctl)[gtid] = 0u;
+  }
+  if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+  if (gtid == 0) {
+    a.dist[a.src] = 0;
+    const uint32_t b = __ldg(a.offs + a.src), e = __ldg(a.offs + a.src + 1);
+    if (!push_binned(a.src, b, e, a.huge, a.queue[0], &a.slots[0].qcount, a.queue_cap,
+                     a.chunks[0], &a.slots[0].ccount, a.chunk_cap))
+      atomicOr(a.err, kErrOverflow);
+  }
+  if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+
+  uint32_t L = 0, T = a.delta, fsel = 0, splits = 0;
+  unsigned long long visits = 0;
+  while (true) {
+    Slot *cur = a.slots + (L & 3u), *nx = a.slots + ((L + 1) & 3u);
+    uint32_t *inq_next = a.inq[(L + 1) % 3];
+    uint32_t *inq_clr = a.inq[(L + 2) % 3];
+    for (uint32_t i = gtid; i < a.W; i += nthreads) inq_clr[i] = 0u;
+    if (gtid < sizeof(Slot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[gtid] = 0u;
+    const uint32_t qc = __ldcg(&cur->qcount), cc = __ldcg(&cur->ccount);
+    RelaxVisitor vis{&a, T, inq_next, a.queue[(L + 1) & 1u], a.far[fsel],
+                     &a.farctl->count[fsel], a.chunks[(L + 1) & 1u], nx, 0ull};
+    expand_binned<kBlock>(a.offs, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, vis);
+    const unsigned long long bv = block_sum_u64<kBlock>(vis.visits);
+    if (threadIdx.x == 0 && bv) atomicAdd(&nx->visits, bv);
+    if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+    visits += __ldcg(&nx->visits);
+    ++L;
+    bool done = false;
+    // near frontier empty: advance the threshold and split the far pile
+    while (__ldcg(&nx->qcount) + __ldcg(&nx->ccount) == 0) {
+      const uint32_t fc = __ldcg(&a.farctl->count[fsel]);
+      if (fc == 0) {
+        done = true;
+        break;
+      }
+      const uint32_t Told = T;
+      uint32_t Tnew = T + a.delta;
+      const uint32_t mf = __ldcg(&a.farctl->minfar[splits & 1u]);
+      if (splits && mf != 0xFFFFFFFFu && mf >= Tnew) Tnew = (mf / a.delta + 1) * a.delta;
+      if (gtid == 0) {
+        a.farctl->count[fsel ^ 1u] = 0u;
+        a.farctl->minfar[(splits + 1) & 1u] = 0xFFFFFFFFu;
+      }
+      if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+      const uint32_t *fp = a.far[fsel];
+      uint32_t *kp = a.far[fsel ^ 1u];
+      uint32_t local_min = 0xFFFFFFFFu;
+      for (uint32_t i = gtid; i < fc; i += nthreads) {
+        const uint32_t v = __ldcg(fp + i);
+        const uint32_t d = __ldcg(a.dist + v);
+        const uint32_t w = v >> 5, bit = 1u << (v & 31u);
+        if (d < Told) {
+          atomicAnd(a.farbm + w, ~bit);  // already expanded from the near frontier
+        } else if (d < Tnew) {
+          atomicAnd(a.farbm + w, ~bit);
+          to_near(a, v, inq_next, a.queue[L & 1u], a.chunks[L & 1u], nx);
+        } else {
+          const uint32_t pos = agg_reserve(&a.farctl->count[fsel ^ 1u]);
+          kp[pos] = v;
+          local_min = min(local_min, d);
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1)
+        local_min = min(local_min, __shfl_down_sync(0xffffffffu, local_min, o));
+      if (lane_id() == 0 && local_min != 0xFFFFFFFFu)
+        atomicMin(&a.farctl->minfar[(splits + 1) & 1u], local_min);
+      T = Tnew;
+      fsel ^= 1u;
+      ++splits;
+      if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+    }
+    if (done) break;
+    if (L > 4u * a.n + 64u) {
+      if (gtid == 0) atomicOr(a.err, kErrLevels);
+      break;
+    }
+  }
+  // epilogue: reached vertices and their out-degree sum (m_r)
+  unsigned long long nr = 0, mr = 0;
+  for (uint32_t v = gtid; v < a.n; v += nthreads)
+    if (__ldcg(a.dist + v) != kInfinit) {
+      ++nr;
+      mr += __ldg(a.offs + v + 1) - __ldg(a.offs + v);
+    }
+  const unsigned long long bnr = block_sum_u64<kBlock>(nr);
+  const unsigned long long bmr = block_sum_u64<kBlock>(mr);
+  if (threadIdx.x == 0) {
+    atomicAdd(&a.summary->nr, bnr);
+    atomicAdd(&a.summary->mr, bmr);
+  }
+  if (gtid == 0) {
+    a.summary->levels = L;
+    a.summary->splits = splits;
+    a.summary->visits = visits;
+  }
+}
+
+}  // namespace
+}  // namespace grus
+
+using namespace grus;
+
+extern "C" int grus_sssp(grus_graph *g, uint32_t src, uint32_t *dist,
+                         grus_stats *stats, void *stream) {
+  if (!g || !dist) return GRUS_EINVAL;
+  if (g->n == 0 || src >= g->n) {
+    set_last_error("source vertex out of range");
+    return GRUS_EINVAL;
+  }
+  if (!g->csr.wts) {
+    set_last_error("sssp needs edge weights (load with need_weights or generate weighted)");
+    return GRUS_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(g->mu);
+  Workspace *w = nullptr;
+  int rc = ws_get(g, &w);
+  if (rc) return rc;
+  const bool dev_out = is_device_pointer(dist);
+  if (!dev_out && !w->dist) GRUS_CUDA_TRY(cudaMalloc(&w->dist, g->n * 4));
+  static int occ = -1;
+  if (occ < 0)
+    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sssp_persistent, kBlock, 0));
+
+  Args a;
+  std::memset(&a, 0, sizeof(a));
+  a.offs = g->csr.offs;
+  a.cols = g->csr.cols;
+  a.wts = g->csr.wts;
+  a.n = (uint32_t)g->n;
+  a.W = w->W;
+  a.src = src;
+  a.dist = dev_out ? dist : w->dist;
+  const uint64_t Wp = ((uint64_t)w->W + 31) / 32 * 32;
+  for (int i = 0; i < 3; ++i) a.inq[i] = w->bitmaps + i * Wp;
+  a.farbm = w->bitmaps + 3 * Wp;
+  a.queue[0] = w->queues;
+  a.queue[1] = w->queues + g->n;
+  a.far[0] = w->far;
+  a.far[1] = w->far + g->n;
+  a.chunks[0] = w->chunks;
+  a.chunks[1] = w->chunks + w->chunk_cap;
+  a.queue_cap = (uint32_t)g->n;
+  a.chunk_cap = w->chunk_cap;
+  a.slots = (Slot *)(w->ctrl + kOffSlots);
+  a.farctl = (FarCtl *)(w->ctrl + kOffFar);
+  a.bar = (GridBarrier *)(w->ctrl + kOffBar);
+  a.err = (uint32_t *)(w->ctrl + kOffErr);
+  a.summary = (Summary *)(w->ctrl + kOffSummary);
+  a.delta = std::max(1u, tune_or(g->tuning.sssp_delta, kDefDelta));
+  a.huge = tune_or(g->tuning.huge_degree, kDefHuge);
+  a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
+
+  const bool sync = stats != nullptr || !dev_out;
+  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffSummary, 0, kCtrlBytes - kOffSummary, s));
+  if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
+  void *args[] = {&a};
+  rc = launch_persistent((const void *)sssp_persistent, args, kBlock,
+                         (int)g->tuning.ctas_per_sm, occ, s, w->bitmaps, w->bitmap_bytes);
+  if (rc) return rc;
+  if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev1, s));
+  if (!dev_out) GRUS_CUDA_TRY(cudaMemcpyAsync(dist, w->dist, g->n * 4, cudaMemcpyDeviceToHost, s));
+  if (!sync) return GRUS_OK;
+  GRUS_CUDA_TRY(cudaMemcpyAsync(w->ctrl_host, w->ctrl, kCtrlBytes, cudaMemcpyDeviceToHost, s));
+  GRUS_CUDA_TRY(cudaStreamSynchronize(s));
+  const uint32_t errbits = *(uint32_t *)(w->ctrl_host + kOffErr);
+  if (errbits) {
+    cudaMemsetAsync(w->ctrl, 0, kCtrlBytes, s);
+    cudaStreamSynchronize(s);
+    return status_from_device_error(errbits);
+  }
+  if (stats) {
+    const Summary *sm = (const Summary *)(w->ctrl_host + kOffSummary);
+    std::memset(stats, 0, sizeof(*stats));
+    stats->levels = sm->levels;
+    stats->direction_switches = sm->splits;  // threshold advances
+    stats->kernel_launches = 1;
+    stats->vertices_reached = sm->nr;
+    stats->edges_reached = sm->mr;
+    stats->edges_relaxed = sm->visits;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+    stats->device_ms = ms;
+  }
+  return GRUS_OK;
+}

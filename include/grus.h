@@ -103,6 +103,7 @@ typedef struct grus_tuning {
   uint32_t huge_degree;   /* degree at/above which a vertex is split into chunks */
   uint32_t bu_scan;       /* neighbours a pull thread checks before deferring */
   uint32_t timeout_ms;    /* bound on every device-side wait */
+  uint32_t sssp_delta;    /* SSSP near/far bucket width (distance units) */
 } grus_tuning;
 
 /* ---- library ------------------------------------------------------------- */
@@ -155,6 +156,29 @@ GRUS_API int grus_graph_free(grus_graph *g);
  * (include/kernel.cuh:124-165): one persistent direction-optimising launch. */
 GRUS_API int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth, grus_stats *stats,
              void *stream);
+
+/* Exact single-source shortest paths over uint32 weights (dist in the same
+ * units; GRUS_INFINIT unreached).  Replaces SSSP_single_gpu
+ * (samples/sssp/sssp.cu:123-170), whose non-atomic relax (:51-60) can lose
+ * updates: here a persistent near/far label-correcting launch with atomicMin.
+ * stats->edges_relaxed counts edge relaxations attempted. */
+GRUS_API int grus_sssp(grus_graph *g, uint32_t src, uint32_t *dist, grus_stats *stats,
+              void *stream);
+
+/* Connected components, label[v] = minimum vertex id of v's component (edges
+ * taken as undirected).  On a symmetric graph this is the fixpoint of the
+ * reference's min-label propagation (samples/cc/cc.cu:69-79, driver :124-190);
+ * computed with a min-hooking union-find (Afforest sampling + giant-component
+ * skip), bit-exact whatever the schedule. */
+GRUS_API int grus_cc(grus_graph *g, uint32_t *label, grus_stats *stats, void *stream);
+
+/* Pull PageRank: r0 = 1/n, r' = (1-d)/n + d * sum r(u)/outdeg(u) over in-edges,
+ * `iters` iterations, FP32 ranks with compensated sums; dangling mass is not
+ * redistributed (samples/pagerank/pr.cu:29-31,83 never pushes from
+ * out-degree-0 vertices).  Builds the CSC on first use.  The reference's own
+ * delta-push PR (pr.cu:17-90) is kept by the drop-in headers. */
+GRUS_API int grus_pagerank(grus_graph *g, float damping, int iters, float *rank,
+                  grus_stats *stats, void *stream);
 
 #ifdef __cplusplus
 }

@@ -60,5 +60,8 @@ def test_package_import_fails_loudly_without_library(tmp_path, monkeypatch):
     shutil.copytree(ROOT / "grus_framework_gb300", pkg, ignore=shutil.ignore_patterns("_lib", "_build", "__pycache__"))
     spec = importlib.util.spec_from_file_location("grus_copy", pkg / "__init__.py")
     mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
     with pytest.raises(ImportError):
-        spec.loader.exec_module(mod)
+        mod.version()
+    with pytest.raises(ImportError):
+        mod.Graph.rmat(8)

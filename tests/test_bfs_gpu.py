@@ -94,8 +94,13 @@ def test_bfs_bins_and_launch_shapes(grus, oracle_mod, huge, bu_scan, ctas):
 
 
 def test_bfs_directed_rmat(grus, oracle_mod):
+    """Directed graph: push-only without a CSC, direction-optimising with one."""
     g = grus.Graph.rmat(14, 16, 3, symmetric=False)
-    _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, 0, 999])
+    srcs = [g.max_degree_vertex, 0, 999]
+    _check_bfs(grus, oracle_mod, g, srcs)
+    g.build_csc()
+    g.set_tuning(alpha=2.0, beta=1e9)  # pull as early as possible
+    _check_bfs(grus, oracle_mod, g, srcs)
 
 
 def test_bfs_grid_high_diameter(grus, oracle_mod):
