@@ -24,6 +24,7 @@
 #include <cstring>
 
 #include "expand.cuh"
+#include "grus_internal.cuh"
 
 namespace grus {
 namespace {

@@ -20,7 +20,7 @@
 //   void edge(uint32_t src, uint32_t aux, uint32_t x)   work on edge index x
 #pragma once
 
-#include "grus_internal.cuh"
+#include "device_util.cuh"
 
 namespace grus {
 
@@ -51,15 +51,89 @@ __device__ __forceinline__ bool push_binned(uint32_t v, uint32_t b, uint32_t e,
   return true;
 }
 
-// Expands the queue tile-by-tile with CTA / warp / gather mappings, then the
-// chunk list one chunk per CTA.  Must be called by every thread of the CTA.
+// One tile: every thread of the CTA brings one source (v, [beg,end), aux);
+// an empty range means "no source".  CTA, warp and gather mappings in turn.
+// Must be called by every thread of the CTA.
+template <int kBlock, class Visitor>
+__device__ __forceinline__ void expand_tile(uint32_t v, uint32_t beg, uint32_t end,
+                                            uint32_t aux, Visitor &vis) {
+  __shared__ uint32_t s_owner, s_src, s_aux, s_beg, s_end;
+  const uint32_t lane = lane_id();
+  // CTA-cooperative
+  while (true) {
+    if (threadIdx.x == 0) s_owner = 0xFFFFFFFFu;
+    __syncthreads();
+    if (end - beg >= kCtaTh) s_owner = threadIdx.x;
+    __syncthreads();
+    const uint32_t owner = s_owner;
+    if (owner == 0xFFFFFFFFu) break;
+    if (threadIdx.x == owner) {
+      s_src = v;
+      s_aux = aux;
+      s_beg = beg;
+      s_end = end;
+      beg = end;
+    }
+    __syncthreads();
+    const uint32_t cs = s_src, ca = s_aux, cb = s_beg, ce = s_end;
+    for (uint32_t x = cb + threadIdx.x; x < ce; x += kBlock) vis.edge(cs, ca, x);
+    __syncthreads();
+  }
+  // warp-cooperative
+  while (true) {
+    const uint32_t ball = __ballot_sync(0xffffffffu, end - beg >= 32);
+    if (!ball) break;
+    const int leader = __ffs(ball) - 1;
+    const uint32_t ws = __shfl_sync(0xffffffffu, v, leader);
+    const uint32_t wa = __shfl_sync(0xffffffffu, aux, leader);
+    const uint32_t wb = __shfl_sync(0xffffffffu, beg, leader);
+    const uint32_t we = __shfl_sync(0xffffffffu, end, leader);
+    if ((int)lane == leader) beg = end;
+    for (uint32_t x = wb + lane; x < we; x += 32) vis.edge(ws, wa, x);
+  }
+  // scan-based gather of the remaining short lists
+  const uint32_t deg = end - beg;
+  uint32_t incl = deg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((int)lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+    const uint32_t k = k0 + lane;
+    int j = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const uint32_t pv = __shfl_sync(0xffffffffu, incl, j + step - 1);
+      if (pv <= k) j += step;
+    }
+    const uint32_t os = __shfl_sync(0xffffffffu, v, j);
+    const uint32_t oa = __shfl_sync(0xffffffffu, aux, j);
+    const uint32_t ob = __shfl_sync(0xffffffffu, beg, j);
+    const uint32_t oi = __shfl_sync(0xffffffffu, incl, j);
+    const uint32_t od = __shfl_sync(0xffffffffu, deg, j);
+    if (k < total) vis.edge(os, oa, ob + (k - (oi - od)));
+  }
+}
+
+// Chunk list: one (v, begin, end) piece per CTA, the whole CTA strides it.
+template <int kBlock, class Visitor>
+__device__ __forceinline__ void expand_chunks(const uint4 *ccur, uint32_t ccount, Visitor &vis) {
+  for (uint32_t c = blockIdx.x; c < ccount; c += gridDim.x) {
+    const uint4 ch = __ldcg(ccur + c);
+    const uint32_t a = vis.aux(ch.x);
+    for (uint32_t x = ch.y + threadIdx.x; x < ch.z; x += kBlock) vis.edge(ch.x, a, x);
+  }
+}
+
+// Expands the queue tile-by-tile, then the chunk list.  Must be called by
+// every thread of the CTA.
 template <int kBlock, class Visitor>
 __device__ __forceinline__ void expand_binned(const uint32_t *__restrict__ offs,
                                               const uint32_t *qcur, uint32_t qcount,
                                               const uint4 *ccur, uint32_t ccount,
                                               Visitor &vis) {
-  __shared__ uint32_t s_owner, s_src, s_aux, s_beg, s_end;
-  const uint32_t lane = lane_id();
   for (uint32_t base = blockIdx.x * kBlock; base < qcount; base += gridDim.x * kBlock) {
     const uint32_t i = base + threadIdx.x;
     uint32_t v = 0, beg = 0, end = 0, aux = 0;
@@ -69,73 +143,9 @@ __device__ __forceinline__ void expand_binned(const uint32_t *__restrict__ offs,
       end = __ldg(offs + v + 1);
       aux = vis.aux(v);
     }
-    // CTA-cooperative
-    while (true) {
-      if (threadIdx.x == 0) s_owner = 0xFFFFFFFFu;
-      __syncthreads();
-      if (end - beg >= kCtaTh) s_owner = threadIdx.x;
-      __syncthreads();
-      const uint32_t owner = s_owner;
-      if (owner == 0xFFFFFFFFu) break;
-      if (threadIdx.x == owner) {
-        s_src = v;
-        s_aux = aux;
-        s_beg = beg;
-        s_end = end;
-        beg = end;
-      }
-      __syncthreads();
-      const uint32_t cs = s_src, ca = s_aux, cb = s_beg, ce = s_end;
-      for (uint32_t x = cb + threadIdx.x; x < ce; x += kBlock) vis.edge(cs, ca, x);
-      __syncthreads();
-    }
-    // warp-cooperative
-    while (true) {
-      const uint32_t ball = __ballot_sync(0xffffffffu, end - beg >= 32);
-      if (!ball) break;
-      const int leader = __ffs(ball) - 1;
-      const uint32_t ws = __shfl_sync(0xffffffffu, v, leader);
-      const uint32_t wa = __shfl_sync(0xffffffffu, aux, leader);
-      const uint32_t wb = __shfl_sync(0xffffffffu, beg, leader);
-      const uint32_t we = __shfl_sync(0xffffffffu, end, leader);
-      if ((int)lane == leader) beg = end;
-      for (uint32_t x = wb + lane; x < we; x += 32) vis.edge(ws, wa, x);
-    }
-    // scan-based gather of the remaining short lists
-    const uint32_t deg = end - beg;
-    uint32_t incl = deg;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-      if ((int)lane >= o) incl += t;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    for (uint32_t k0 = 0; k0 < total; k0 += 32) {
-      const uint32_t k = k0 + lane;
-      int j = 0;
-#pragma unroll
-      for (int step = 16; step >= 1; step >>= 1) {
-        const uint32_t pv = __shfl_sync(0xffffffffu, incl, j + step - 1);
-        if (pv <= k) j += step;
-      }
-      const uint32_t os = __shfl_sync(0xffffffffu, v, j);
-      const uint32_t oa = __shfl_sync(0xffffffffu, aux, j);
-      const uint32_t ob = __shfl_sync(0xffffffffu, beg, j);
-      const uint32_t oi = __shfl_sync(0xffffffffu, incl, j);
-      const uint32_t od = __shfl_sync(0xffffffffu, deg, j);
-      if (k < total) vis.edge(os, oa, ob + (k - (oi - od)));
-    }
+    expand_tile<kBlock>(v, beg, end, aux, vis);
   }
-  for (uint32_t c = blockIdx.x; c < ccount; c += gridDim.x) {
-    const uint4 ch = __ldcg(ccur + c);
-    const uint32_t a = vis.aux(ch.x);
-    for (uint32_t x = ch.y + threadIdx.x; x < ch.z; x += kBlock) vis.edge(ch.x, a, x);
-  }
+  expand_chunks<kBlock>(ccur, ccount, vis);
 }
-
-// Launch helper for persistent cooperative kernels: SMs x min(occupancy,
-// requested) CTAs, with an optional L2 persisting window over `win_base`.
-int launch_persistent(const void *fn, void **args, int block, int per_sm_req,
-                      int occupancy, cudaStream_t s, void *win_base, size_t win_bytes);
 
 }  // namespace grus

@@ -28,10 +28,6 @@
 
 namespace grus {
 
-int build_csc_locked(grus_graph *g);
-int launch_persistent(const void *fn, void **args, int block, int per_sm_req,
-                      int occupancy, cudaStream_t s, void *win_base, size_t win_bytes);
-
 namespace {
 
 constexpr int kBlock = 256;
