@@ -535,3 +535,161 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   }
   return GRUS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// grus_bfs_static: the same persistent BFS with no allocation at call time.
+//
+// Some callers cannot call cudaMalloc: code embedded in a host process that
+// owns the whole device-memory budget through its own pool (or holds the free
+// HBM in a balloon, as this library's managed mode does, so any new
+// allocation would fail), and latency-critical loops where cudaMalloc/cudaFree
+// would synchronise the device and stall work on other streams.  For them
+// the scratch (frontier bitmaps, queues, chunk lists, control block) lives in
+// one file-scope __device__ array of fixed size, sized for graphs of up to
+// GRUS_STATIC_MAX_VERTICES vertices and GRUS_STATIC_MAX_EDGES edges.  Every
+// GPU that loads this library holds that array until the process exits.
+//
+// Host code cannot use the array's name as a device address (in host code it
+// names a host-side stand-in), so the first call on each device looks the
+// address up with cudaGetSymbolAddress while that device is current and
+// caches it; make that first call before any stream capture.  All calls on a
+// device share the array and it keeps the last call's contents: each call
+// clears its control block, and the kernel's prologue clears the bitmaps and
+// level slots.  Calls that overlap on the GPU (different streams or threads,
+// same device) race on the array and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+namespace grus {
+namespace {
+
+constexpr uint64_t kStaticMaxN = GRUS_STATIC_MAX_VERTICES;
+constexpr uint64_t kStaticMaxM = GRUS_STATIC_MAX_EDGES;
+constexpr uint64_t kStaticWp = ((kStaticMaxN + 31) / 32 + 31) / 32 * 32;
+constexpr uint64_t kStaticChunkCap = kStaticMaxM / kChunk + kStaticMaxM / kDefHuge + 2;
+constexpr size_t kStaticBitmapOff = kCtrlBytes;
+constexpr size_t kStaticQueueOff = kStaticBitmapOff + 4 * kStaticWp * 4;
+constexpr size_t kStaticChunkOff = kStaticQueueOff + 2 * kStaticMaxN * 4;
+constexpr size_t kStaticBytes = kStaticChunkOff + 2 * kStaticChunkCap * sizeof(uint4);
+static_assert(kStaticBitmapOff % 256 == 0 && kStaticQueueOff % 256 == 0 &&
+                  kStaticChunkOff % 256 == 0,
+              "scratch sections must stay 256-byte aligned");
+
+// [control block | visited + 3 frontier bitmaps | 2 queues | 2 chunk lists]
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+std::mutex g_static_mu;
+void *g_static_base[64] = {};
+int g_static_occ = -1;
+
+// Device address of g_static_scratch on the current device (looked up once).
+int static_scratch(void **base) {
+  int dev = 0;
+  GRUS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return GRUS_ENODEV;
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_base[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p) {
+      set_last_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+      return status_from_cuda(e == cudaSuccess ? cudaErrorInvalidSymbol : e);
+    }
+    g_static_base[dev] = p;
+  }
+  if (g_static_occ < 0)
+    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_static_occ, bfs_persistent, kBlock, 0));
+  *base = g_static_base[dev];
+  return GRUS_OK;
+}
+
+}  // namespace
+}  // namespace grus
+
+extern "C" int grus_bfs_static(uint64_t n, uint64_t m, const uint32_t *offsets,
+                               const uint32_t *cols, int symmetric, uint32_t src,
+                               uint32_t *depth, grus_stats *stats, void *stream) {
+  if (!offsets || (m && !cols) || !depth) return GRUS_EINVAL;
+  if (n > kStaticMaxN || m > kStaticMaxM) {
+    set_last_error("grus_bfs_static handles at most GRUS_STATIC_MAX_VERTICES (2^20) vertices "
+                   "and GRUS_STATIC_MAX_EDGES (2^25) edges; use grus_bfs for larger graphs");
+    return GRUS_EOVERFLOW;
+  }
+  if (n == 0 || src >= n) {
+    set_last_error("source vertex out of range");
+    return GRUS_EINVAL;
+  }
+  if (!is_device_pointer(offsets) || (m && !is_device_pointer(cols)) || !is_device_pointer(depth)) {
+    set_last_error("grus_bfs_static needs device (or managed) offsets, cols and depth");
+    return GRUS_EINVAL;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  void *base = nullptr;
+  int rc = static_scratch(&base);
+  if (rc) return rc;
+  char *ctrl = (char *)base;
+  uint32_t *bitmaps = (uint32_t *)((char *)base + kStaticBitmapOff);
+  uint32_t *queues = (uint32_t *)((char *)base + kStaticQueueOff);
+  uint4 *chunks = (uint4 *)((char *)base + kStaticChunkOff);
+  const uint32_t W = (uint32_t)((n + 31) / 32);
+  const uint64_t Wp = ((uint64_t)W + 31) / 32 * 32;
+
+  Args a;
+  std::memset(&a, 0, sizeof(a));
+  a.offs = offsets;
+  a.cols = cols;
+  a.ioffs = symmetric ? offsets : nullptr;
+  a.icols = symmetric ? cols : nullptr;
+  a.allow_pull = symmetric != 0;
+  a.n = (uint32_t)n;
+  a.W = W;
+  a.m = m;
+  a.src = src;
+  a.depth = depth;
+  a.visited = bitmaps;
+  a.front[0] = bitmaps + Wp;
+  a.front[1] = bitmaps + 2 * Wp;
+  a.front[2] = bitmaps + 3 * Wp;
+  a.queue[0] = queues;
+  a.queue[1] = queues + n;
+  a.chunk_cap = (uint32_t)(m / kChunk + m / kDefHuge + 2);
+  a.chunks[0] = chunks;
+  a.chunks[1] = chunks + a.chunk_cap;
+  a.queue_cap = (uint32_t)n;
+  a.slots = (LevelSlot *)(ctrl + kOffSlots);
+  a.bar = (GridBarrier *)(ctrl + kOffBar);
+  a.err = (uint32_t *)(ctrl + kOffErr);
+  a.summary = (Summary *)(ctrl + kOffSummary);
+  a.alpha = kDefAlpha;
+  a.beta = kDefBeta;
+  a.huge = kDefHuge;
+  a.bu_scan = kDefBuScan;
+  a.timeout_ns = 30000ull * 1000000ull;
+
+  // the array keeps the previous call's control block: start from zero
+  GRUS_CUDA_TRY(cudaMemsetAsync(ctrl, 0, kCtrlBytes, s));
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeCooperative;
+  attr.val.cooperative = 1;
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)(device_sm_count() * std::max(g_static_occ, 1)));
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = s;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, bfs_persistent, a));
+  if (!stats) return GRUS_OK;
+  unsigned char host_ctrl[kCtrlBytes];  // pageable stack copy: no allocation
+  GRUS_CUDA_TRY(cudaMemcpyAsync(host_ctrl, ctrl, kCtrlBytes, cudaMemcpyDeviceToHost, s));
+  GRUS_CUDA_TRY(cudaStreamSynchronize(s));
+  const uint32_t errbits = *(const uint32_t *)(host_ctrl + kOffErr);
+  if (errbits) return status_from_device_error(errbits);
+  const Summary *sm = (const Summary *)(host_ctrl + kOffSummary);
+  std::memset(stats, 0, sizeof(*stats));
+  stats->levels = sm->levels;
+  stats->bottom_up_levels = sm->bu_levels;
+  stats->direction_switches = sm->switches;
+  stats->kernel_launches = 1;
+  stats->vertices_reached = sm->nr;
+  stats->edges_reached = sm->mr;
+  return GRUS_OK;
+}

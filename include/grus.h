@@ -157,6 +157,25 @@ GRUS_API int grus_graph_free(grus_graph *g);
 GRUS_API int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth, grus_stats *stats,
              void *stream);
 
+/* Allocation-free BFS.  No counterpart in the reference.  For callers that
+ * cannot allocate device memory (a host process that owns the whole device
+ * budget through its own pool, or loops where cudaMalloc's device-wide
+ * synchronisation is not acceptable): same algorithm and results as
+ * grus_bfs, but on raw device CSR arrays (offsets, cols, depth must be device
+ * or managed memory; `symmetric` != 0 lets pull levels use the CSR as
+ * in-edges, else the BFS runs push-only) with its scratch in a fixed
+ * file-scope device array held by every GPU that loads the library (about
+ * 9 MB).  Graphs above the limits below are rejected with GRUS_EOVERFLOW.
+ * The first call on a device looks the array up (make it before any stream
+ * capture).  All calls share the array: calls that overlap on the GPU race.
+ * Asynchronous on `stream` unless `stats` is given (then it waits and reports
+ * device-side errors). */
+#define GRUS_STATIC_MAX_VERTICES (1u << 20)
+#define GRUS_STATIC_MAX_EDGES (1u << 25)
+GRUS_API int grus_bfs_static(uint64_t n, uint64_t m, const uint32_t *offsets,
+                    const uint32_t *cols, int symmetric, uint32_t src, uint32_t *depth,
+                    grus_stats *stats, void *stream);
+
 /* Exact single-source shortest paths over uint32 weights (dist in the same
  * units; GRUS_INFINIT unreached).  Replaces SSSP_single_gpu
  * (samples/sssp/sssp.cu:123-170), whose non-atomic relax (:51-60) can lose

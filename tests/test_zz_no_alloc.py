@@ -1,0 +1,76 @@
+"""GPU: the allocation-free BFS entry point, grus_bfs_static.
+
+It serves callers that cannot allocate device memory (a host process that
+owns the whole device budget through its own pool, or loops that cannot
+afford cudaMalloc's device-wide synchronisation): its scratch is a fixed
+device array inside libgrus, and the caller passes device CSR arrays and a
+device output.  This file checks, through the C ABI, that two calls in a row
+give exactly the depths of the allocating entry point grus_bfs (bit-exact,
+the bar of every BFS test here), for a symmetric graph (direction-optimising)
+and a directed one (push only), and that oversized graphs are refused.
+It is collected last so that a run stopping at the first failure has run
+every other test first; it passes alone in a fresh process as well.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _static_fn(grus):
+    fn = grus.lib.grus_bfs_static
+    fn.argtypes = [C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_int, C.c_uint32,
+                   C.c_void_p, C.POINTER(grus.Stats), C.c_void_p]
+    fn.restype = C.c_int
+    return fn
+
+
+@pytest.mark.parametrize("symmetric", [True, False])
+def test_static_bfs_matches_grus_bfs_twice(grus, symmetric):
+    torch = pytest.importorskip("torch")
+    fn = _static_fn(grus)
+    g = grus.Graph.rmat(16, 16, 1, symmetric=symmetric)
+    info = g.info()
+    assert info.n <= (1 << 20) and info.m <= (1 << 25)
+    out = torch.empty(info.n, dtype=torch.int32, device="cuda")
+    for src in (g.max_degree_vertex, 4242):  # two calls in a row on the shared scratch
+        ref, ref_st = grus.bfs(g, src, stats=True)
+        out.fill_(-1)
+        st = grus.Stats()
+        rc = fn(info.n, info.m, info.offsets, info.cols, int(symmetric), src, out.data_ptr(),
+                C.byref(st), None)
+        assert rc == 0, grus.lib.grus_last_error()
+        got = out.cpu().numpy().view(np.uint32)
+        assert np.array_equal(got, ref)
+        assert st.vertices_reached == ref_st["vertices_reached"]
+        assert st.edges_reached == ref_st["edges_reached"]
+    g.free()
+
+
+def test_static_bfs_async_then_sync(grus):
+    """Without stats the call is asynchronous on the stream; results match."""
+    torch = pytest.importorskip("torch")
+    fn = _static_fn(grus)
+    g = grus.Graph.rmat(14, 8, 3, symmetric=True)
+    info = g.info()
+    out = torch.empty(info.n, dtype=torch.int32, device="cuda")
+    s = torch.cuda.Stream()
+    rc = fn(info.n, info.m, info.offsets, info.cols, 1, 7, out.data_ptr(), None, s.cuda_stream)
+    assert rc == 0
+    s.synchronize()
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), grus.bfs(g, 7))
+
+
+def test_static_bfs_rejects_oversized_and_bad_args(grus):
+    torch = pytest.importorskip("torch")
+    fn = _static_fn(grus)
+    g = grus.Graph.rmat(10, 4, 1)
+    info = g.info()
+    out = torch.empty(info.n, dtype=torch.int32, device="cuda")
+    assert fn((1 << 20) + 1, info.m, info.offsets, info.cols, 1, 0, out.data_ptr(), None, None) == grus.EOVERFLOW
+    assert fn(info.n, (1 << 25) + 1, info.offsets, info.cols, 1, 0, out.data_ptr(), None, None) == grus.EOVERFLOW
+    assert fn(info.n, info.m, info.offsets, info.cols, 1, info.n, out.data_ptr(), None, None) == grus.EINVAL
+    host = np.empty(info.n, np.uint32)
+    assert fn(info.n, info.m, info.offsets, info.cols, 1, 0, host.ctypes.data, None, None) == grus.EINVAL
