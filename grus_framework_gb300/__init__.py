@@ -65,11 +65,16 @@ class GraphInfo(C.Structure):
     ]
 
 
+class LevelTrace(C.Structure):
+    _fields_ = [("end_ns", C.c_uint64), ("edges", C.c_uint64), ("vertices", C.c_uint32),
+                ("pull", C.c_uint32)]
+
+
 class Tuning(C.Structure):
     _fields_ = [
         ("alpha", C.c_float), ("beta", C.c_float), ("ctas_per_sm", C.c_uint32),
         ("huge_degree", C.c_uint32), ("bu_scan", C.c_uint32), ("timeout_ms", C.c_uint32),
-        ("sssp_delta", C.c_uint32),
+        ("sssp_delta", C.c_uint32), ("bu_words", C.c_uint32),
     ]
 
 
@@ -100,6 +105,7 @@ def _load():
         "grus_graph_free": ([vp], i32),
         "grus_bfs": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
         "grus_sssp": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
+        "grus_bfs_trace": ([vp, C.POINTER(LevelTrace), i32], i32),
         "grus_cc": ([vp, vp, C.POINTER(Stats), vp], i32),
         "grus_pagerank": ([vp, C.c_float, i32, vp, C.POINTER(Stats), vp], i32),
     }
@@ -317,6 +323,16 @@ def bfs(g: Graph, src: int, out=None, stream=None, stats: bool = False):
     _check(lib.grus_bfs(g._handle(), src, _ptr(out), C.byref(st) if st is not None else None,
                         _stream(stream)), "grus_bfs")
     return (out, st.as_dict()) if stats else out
+
+
+def bfs_trace(g: Graph, max_levels: int = 128):
+    """Per-level records of the last bfs(..., stats=True) call on `g`."""
+    buf = (LevelTrace * max_levels)()
+    k = lib.grus_bfs_trace(g._handle(), buf, max_levels)
+    if k < 0:
+        _check(k, "grus_bfs_trace")
+    return [dict(end_us=buf[i].end_ns / 1e3, edges=buf[i].edges, vertices=buf[i].vertices,
+                 pull=bool(buf[i].pull)) for i in range(k)]
 
 
 def sssp(g: Graph, src: int, out=None, stream=None, stats: bool = False):

@@ -25,15 +25,15 @@
 //   * pull (bottom-up) levels: a warp owns 32 consecutive vertices (one bitmap
 //     word); each unvisited vertex scans its first `bu_scan` neighbours four at
 //     a time and stops at the first frontier parent; longer unresolved lists
-//     are deferred to a CTA list and finished warp-cooperatively (32
-//     neighbours per ballot).  The word's next-frontier and visited bits are
-//     written with one store per warp.
+//     are finished by the whole warp (32 neighbours per ballot).  The word's
+//     next-frontier and visited bits are written with one store per warp.
 //   * pull levels read in-edges: the CSR itself on a symmetric graph, the CSC
 //     (grus_graph_build_csc) on a directed one; without a CSC a directed graph
 //     runs push-only.
-//   * direction: Beamer's heuristic -- push->pull when m_f > m_u/alpha,
-//     pull->push when n_f < n/beta and the frontier shrinks; switching back to
-//     push compacts the frontier bitmap into the binned queue.
+//   * direction: Beamer's heuristic -- push->pull when the frontier grows and
+//     m_f > m_u/alpha, pull->push when n_f < n/beta and the frontier shrinks;
+//     the first push level after a pull level reads its sources straight from
+//     the frontier bitmap.
 // Depths are order-independent (every writer stores level+1), so results are
 // bit-exact against the serial oracle whatever the schedule.
 #include <algorithm>
@@ -48,8 +48,8 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 constexpr uint32_t kDefHuge = 8192;   // chunking threshold
-constexpr uint32_t kDefBuScan = 8;    // pull: neighbours checked before deferring
-constexpr int kDeferCap = 1024;       // pull: deferred vertices per CTA
+constexpr uint32_t kDefBuScan = 8;    // pull: neighbours a lane checks alone
+constexpr uint32_t kDefBuWords = 4;   // pull: bitmap words per warp step
 constexpr float kDefAlpha = 15.f, kDefBeta = 18.f;
 
 struct LevelSlot {
@@ -64,6 +64,15 @@ struct LevelSlot {
 struct Summary {
   uint32_t levels, bu_levels, switches, pad;
   unsigned long long nr, mr;
+};
+
+// Per-level record written by one thread after each level's barrier:
+// entry 0 holds the kernel start time, entry L+1 the end of level L.
+constexpr int kMaxTrace = 128;
+struct LevelTrace {
+  unsigned long long t_ns;
+  unsigned long long mf;
+  uint32_t nf, pull;
 };
 
 struct Args {
@@ -85,6 +94,7 @@ struct Args {
   GridBarrier *bar;
   uint32_t *err;
   Summary *summary;
+  LevelTrace *trace;      // optional (null: no trace)
   float alpha, beta;
   uint32_t huge, bu_scan;
   uint64_t timeout_ns;
@@ -101,6 +111,9 @@ struct Workspace {
   uint32_t chunk_cap = 0;
   char *ctrl = nullptr;          // slots, barrier, err, summary
   char *ctrl_host = nullptr;     // pinned mirror for readback
+  LevelTrace *trace = nullptr;   // device per-level records
+  LevelTrace *trace_host = nullptr;
+  int trace_levels = 0;          // records valid in trace_host
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -115,7 +128,9 @@ void ws_free(void *p) {
   cudaFree(w->queues);
   cudaFree(w->chunks);
   cudaFree(w->ctrl);
+  cudaFree(w->trace);
   if (w->ctrl_host) cudaFreeHost(w->ctrl_host);
+  if (w->trace_host) cudaFreeHost(w->trace_host);
   if (w->ev0) cudaEventDestroy(w->ev0);
   if (w->ev1) cudaEventDestroy(w->ev1);
   delete w;
@@ -141,6 +156,8 @@ int ws_get(grus_graph *g, Workspace **out) {
   if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
   if (e == cudaSuccess) e = cudaMemset(w->ctrl, 0, kCtrlBytes);
   if (e == cudaSuccess) e = cudaMallocHost(&w->ctrl_host, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&w->trace, kMaxTrace * sizeof(LevelTrace));
+  if (e == cudaSuccess) e = cudaMallocHost(&w->trace_host, kMaxTrace * sizeof(LevelTrace));
   if (e == cudaSuccess) e = cudaEventCreate(&w->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&w->ev1);
   if (e != cudaSuccess) {
@@ -198,125 +215,116 @@ __device__ __forceinline__ void enqueue_binned(const Args &a, uint32_t v,
 // ---------------------------------------------------------------------------
 // pull level
 // ---------------------------------------------------------------------------
-struct PullShared {
-  uint32_t ndef;
-  uint4 def[kDeferCap];  // (v, next edge, end, begin)
-};
-
-__device__ __forceinline__ void bu_drain(const Args &a, PullShared &sh, uint32_t nd,
-                                         const uint32_t *fcur, uint32_t *fnext,
-                                         uint32_t &nf, unsigned long long &mf) {
-  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-  const uint32_t cnt = min(sh.ndef, (uint32_t)kDeferCap);
-  for (uint32_t j = warp; j < cnt; j += kWarps) {
-    const uint4 d = sh.def[j];
-    bool hit = false;
-    for (uint32_t base = d.y; base < d.z; base += 32) {
-      const uint32_t x = base + lane;
-      const bool h = x < d.z && test_bit(fcur, __ldg(a.icols + x));
-      if (__ballot_sync(0xffffffffu, h)) {
-        hit = true;
-        break;
-      }
-    }
-    if (hit && lane == 0) {
-      const uint32_t v = d.x, bit = 1u << (v & 31u);
-      a.depth[v] = nd;
-      atomicOr(a.visited + (v >> 5), bit);
-      atomicOr(fnext + (v >> 5), bit);
-      nf += 1;
-      mf += __ldg(a.offs + v + 1) - __ldg(a.offs + v);
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) sh.ndef = 0;
-  __syncthreads();
-}
-
-__device__ __forceinline__ void bu_level(const Args &a, PullShared &sh, uint32_t L,
-                                         const uint32_t *fcur, uint32_t *fnext,
-                                         uint32_t &nf, unsigned long long &mf) {
+// A warp owns K consecutive bitmap words (32 vertices each) per
+// step and interleaves their load chains (visited words, offsets, the first
+// neighbours, their frontier bits) so several memory round trips are in
+// flight per warp.  Each unvisited lane checks its first `bu_scan`
+// in-neighbours, four at a time; lanes whose list is longer and still
+// unresolved are then finished by the whole warp, 32 neighbours per ballot.
+// Everything is warp-synchronous: no block barrier inside a pull level.
+template <int K>
+__device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32_t *fcur,
+                                         uint32_t *fnext, uint32_t &nf, unsigned long long &mf) {
   const uint32_t nd = L + 1;
-  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-  const uint32_t scan = a.bu_scan;
-  for (uint32_t tile = blockIdx.x; tile * kWarps < a.W; tile += gridDim.x) {
-    const uint32_t w = tile * kWarps + warp;
-    if (w < a.W) {
-      const uint32_t vis = __ldcg(a.visited + w);
-      if (vis != 0xFFFFFFFFu) {
-        const uint32_t v = w * 32 + lane;
-        const bool active = !((vis >> lane) & 1u) && v < a.n;
-        bool found = false;
-        uint32_t b = 0, e = 0;
-        if (active) {
-          b = __ldg(a.ioffs + v);
-          e = __ldg(a.ioffs + v + 1);
-          const uint32_t lim = min(e, b + scan);
-          uint32_t x = b;
-          for (; x < lim; x += 4) {
-            // four independent loads in flight, then four bitmap probes
-            uint32_t u0 = __ldg(a.icols + x);
-            uint32_t u1 = x + 1 < lim ? __ldg(a.icols + x + 1) : u0;
-            uint32_t u2 = x + 2 < lim ? __ldg(a.icols + x + 2) : u0;
-            uint32_t u3 = x + 3 < lim ? __ldg(a.icols + x + 3) : u0;
-            if (test_bit(fcur, u0) | test_bit(fcur, u1) | test_bit(fcur, u2) |
-                test_bit(fcur, u3)) {
-              found = true;
-              break;
-            }
-          }
-          if (!found && lim < e) {
-            const uint32_t pos = atomicAdd(&sh.ndef, 1u);
-            if (pos < (uint32_t)kDeferCap) {
-              sh.def[pos] = make_uint4(v, lim, e, b);
-            } else {
-              for (x = lim; x < e; ++x)
-                if (test_bit(fcur, __ldg(a.icols + x))) {
-                  found = true;
-                  break;
-                }
-            }
-          }
-        }
-        const uint32_t mask = __ballot_sync(0xffffffffu, found);
-        if (mask) {
-          if (lane == 0) {
-            a.visited[w] = vis | mask;
-            fnext[w] = mask;
-          }
-          if (found) {
-            a.depth[v] = nd;
-            nf += 1;
-            mf += __ldg(a.offs + v + 1) - __ldg(a.offs + v);
-          }
-        }
-      }
-    }
-    __syncthreads();
-    if (sh.ndef > (uint32_t)(kDeferCap - kBlock)) bu_drain(a, sh, nd, fcur, fnext, nf, mf);
-  }
-  __syncthreads();
-  bu_drain(a, sh, nd, fcur, fnext, nf, mf);
-}
-
-// pull -> push: turn the next-frontier bitmap into the binned queue
-__device__ __forceinline__ void bitmap_to_queue(const Args &a, const uint32_t *fmap,
-                                                uint32_t *qnext, uint4 *cnext,
-                                                LevelSlot *nx) {
   const uint32_t lane = lane_id();
+  const uint32_t scan = a.bu_scan;
   const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * kBlock) >> 5;
-  for (uint32_t w = gw; w < a.W; w += nw) {
-    const uint32_t word = __ldcg(fmap + w);
-    if (word && ((word >> lane) & 1u)) enqueue_binned(a, w * 32 + lane, qnext, cnext, nx);
+  for (uint32_t w0 = gw * K; w0 < a.W; w0 += nw * K) {
+    uint32_t vis[K], b[K], e[K], lim[K];
+    bool act[K], found[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) vis[k] = w0 + k < a.W ? __ldcg(a.visited + w0 + k) : 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint32_t v = (w0 + k) * 32 + lane;
+      act[k] = !((vis[k] >> lane) & 1u) && v < a.n;
+      found[k] = false;
+      b[k] = e[k] = lim[k] = 0;
+      if (act[k]) {
+        b[k] = __ldg(a.ioffs + v);
+        e[k] = __ldg(a.ioffs + v + 1);
+        lim[k] = min(e[k], b[k] + scan);
+      }
+    }
+    // probe rounds: four neighbours per word, K words at once
+    for (uint32_t r = 0; r < scan; r += 4) {
+      uint32_t u[K][4];
+      bool any = false;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const uint32_t x = b[k] + r;
+        const bool go = act[k] && !found[k] && x < lim[k];
+        any |= go;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          u[k][j] = go && x + j < lim[k] ? __ldg(a.icols + x + j) : 0xFFFFFFFFu;
+      }
+      if (!__any_sync(0xffffffffu, any)) break;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        bool h = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) h |= u[k][j] != 0xFFFFFFFFu && test_bit(fcur, u[k][j]);
+        found[k] |= h;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      uint32_t pending = __ballot_sync(0xffffffffu, act[k] && !found[k] && lim[k] < e[k]);
+      while (pending) {
+        const int j = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const uint32_t jb = __shfl_sync(0xffffffffu, lim[k], j);
+        const uint32_t je = __shfl_sync(0xffffffffu, e[k], j);
+        for (uint32_t base = jb; base < je; base += 32) {
+          const uint32_t x = base + lane;
+          const bool h = x < je && test_bit(fcur, __ldg(a.icols + x));
+          if (__ballot_sync(0xffffffffu, h)) {
+            if ((int)lane == j) found[k] = true;
+            break;
+          }
+        }
+      }
+      const uint32_t mask = __ballot_sync(0xffffffffu, found[k]);
+      if (mask) {
+        const uint32_t w = w0 + k, v = w * 32 + lane;
+        if (lane == 0) {
+          a.visited[w] = vis[k] | mask;
+          fnext[w] = mask;
+        }
+        if (found[k]) {
+          a.depth[v] = nd;
+          nf += 1;
+          mf += __ldg(a.offs + v + 1) - __ldg(a.offs + v);
+        }
+      }
+    }
   }
 }
 
+// First push level after a pull level: its frontier exists only as the
+// bitmap `fcur`, so the sources are the vertex ids whose bit is set, expanded
+// tile by tile with the same binned mappings (no queue conversion, no extra
+// barrier).
+__device__ __forceinline__ void td_from_bitmap(const Args &a, const uint32_t *fcur,
+                                               PushVisitor &vis) {
+  for (uint32_t base = blockIdx.x * kBlock; base < a.n; base += gridDim.x * kBlock) {
+    const uint32_t v = base + threadIdx.x;
+    uint32_t beg = 0, end = 0;
+    if (v < a.n && test_bit(fcur, v)) {
+      beg = __ldg(a.offs + v);
+      end = __ldg(a.offs + v + 1);
+    }
+    expand_tile<kBlock>(v, beg, end, 0u, vis);
+  }
+}
+
+template <int K>
 __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
-  __shared__ PullShared sh;
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
-  if (threadIdx.x == 0) sh.ndef = 0;
+  if (gtid == 0 && a.trace) a.trace[0] = LevelTrace{global_timer_ns(), 0ull, 1u, 0u};
   // prologue: clear the bitmaps and the level slots
   {
     uint32_t *bm = a.visited;
@@ -336,7 +344,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
   if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
 
   uint32_t L = 0;
-  bool bu = false;
+  bool bu = false, from_pull = false;
   uint64_t mu = a.m - (uint64_t)(se - sb);
   uint32_t prev_nf = 1, bu_levels = 0, switches = 0;
   unsigned long long nr = 1, mr = se - sb;
@@ -351,13 +359,17 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     uint32_t nf = 0;
     unsigned long long mf = 0;
     if (!bu) {
-      const uint32_t qc = __ldcg(&cur->qcount), cc = __ldcg(&cur->ccount);
       PushVisitor vis{&a, L + 1, fnext, a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx, 0u, 0ull};
-      expand_binned<kBlock>(a.offs, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, vis);
+      if (from_pull) {
+        td_from_bitmap(a, fcur, vis);
+      } else {
+        const uint32_t qc = __ldcg(&cur->qcount), cc = __ldcg(&cur->ccount);
+        expand_binned<kBlock>(a.offs, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, vis);
+      }
       nf = vis.nf;
       mf = vis.mf;
     } else {
-      bu_level(a, sh, L, fcur, fnext, nf, mf);
+      bu_level<K>(a, L, fcur, fnext, nf, mf);
     }
     const unsigned long long bnf = block_sum_u64<kBlock>(nf);
     const unsigned long long bmf = block_sum_u64<kBlock>(mf);
@@ -368,6 +380,8 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
     const uint32_t NF = __ldcg(&nx->nf);
     const unsigned long long MF = __ldcg(&nx->mf);
+    if (gtid == 0 && a.trace && L + 1 < (uint32_t)kMaxTrace)
+      a.trace[L + 1] = LevelTrace{global_timer_ns(), MF, NF, bu ? 1u : 0u};
     if (bu) ++bu_levels;
     if (NF == 0) break;
     nr += NF;
@@ -375,14 +389,12 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     mu = mu > MF ? mu - MF : 0;
     bool nbu = bu;
     if (!bu) {
-      if (a.allow_pull && (double)MF * a.alpha > (double)mu) nbu = true;
+      // push -> pull while the frontier grows and its edges outweigh m_u/alpha
+      if (a.allow_pull && NF > prev_nf && (double)MF * a.alpha > (double)mu) nbu = true;
     } else {
       if ((double)NF * a.beta < (double)a.n && NF < prev_nf) nbu = false;
     }
-    if (bu && !nbu) {
-      bitmap_to_queue(a, fnext, a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx);
-      if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-    }
+    from_pull = bu && !nbu;
     if (nbu != bu) ++switches;
     bu = nbu;
     prev_nf = NF;
@@ -431,9 +443,14 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   const bool dev_out = is_device_pointer(depth);
   if (!dev_out && !w->depth) GRUS_CUDA_TRY(cudaMalloc(&w->depth, g->n * 4));
 
-  static int occ = -1;
+  // pull-level words per warp step: 2 (more resident warps) or 4 (more
+  // loads in flight per warp)
+  const bool wide = tune_or(g->tuning.bu_words, kDefBuWords) >= 4;
+  auto kern = wide ? bfs_persistent<4> : bfs_persistent<2>;
+  static int occ_tab[2] = {-1, -1};
+  int &occ = occ_tab[wide ? 1 : 0];
   if (occ < 0) {
-    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bfs_persistent, kBlock, 0));
+    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kBlock, 0));
   }
   const int sms = device_sm_count();
   int per_sm = occ;
@@ -475,6 +492,7 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   a.bar = (GridBarrier *)(w->ctrl + kOffBar);
   a.err = (uint32_t *)(w->ctrl + kOffErr);
   a.summary = (Summary *)(w->ctrl + kOffSummary);
+  a.trace = w->trace;
   a.alpha = tune_or(g->tuning.alpha, kDefAlpha);
   a.beta = tune_or(g->tuning.beta, kDefBeta);
   a.huge = tune_or(g->tuning.huge_degree, kDefHuge);
@@ -507,12 +525,15 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
 
   const bool sync = stats != nullptr || !dev_out;
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
-  GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, bfs_persistent, a));
+  GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a));
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev1, s));
   if (!dev_out) GRUS_CUDA_TRY(cudaMemcpyAsync(depth, w->depth, g->n * 4, cudaMemcpyDeviceToHost, s));
   if (!sync) return GRUS_OK;
   GRUS_CUDA_TRY(cudaMemcpyAsync(w->ctrl_host, w->ctrl, kCtrlBytes, cudaMemcpyDeviceToHost, s));
+  GRUS_CUDA_TRY(cudaMemcpyAsync(w->trace_host, w->trace, kMaxTrace * sizeof(LevelTrace),
+                                cudaMemcpyDeviceToHost, s));
   GRUS_CUDA_TRY(cudaStreamSynchronize(s));
+  w->trace_levels = std::min<int>(((const Summary *)(w->ctrl_host + kOffSummary))->levels + 1, kMaxTrace);
   const uint32_t errbits = *(uint32_t *)(w->ctrl_host + kOffErr);
   if (errbits) {
     // reset the control block so the next call starts clean
@@ -534,6 +555,23 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
     stats->device_ms = ms;
   }
   return GRUS_OK;
+}
+
+extern "C" int grus_bfs_trace(grus_graph *g, grus_level_trace *out, int max_levels) {
+  if (!g || !out || max_levels < 0) return GRUS_EINVAL;
+  std::lock_guard<std::mutex> lk(g->mu);
+  const Workspace *w = (const Workspace *)g->ws[kWsBfs];
+  if (!w || w->trace_levels < 2) return 0;
+  const int levels = std::min(w->trace_levels - 1, max_levels);
+  const uint64_t t0 = w->trace_host[0].t_ns;
+  for (int i = 0; i < levels; ++i) {
+    const LevelTrace &r = w->trace_host[i + 1];
+    out[i].end_ns = r.t_ns - t0;
+    out[i].edges = r.mf;
+    out[i].vertices = r.nf;
+    out[i].pull = r.pull;
+  }
+  return levels;
 }
 
 // ---------------------------------------------------------------------------
@@ -596,7 +634,7 @@ int static_scratch(void **base) {
     g_static_base[dev] = p;
   }
   if (g_static_occ < 0)
-    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_static_occ, bfs_persistent, kBlock, 0));
+    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_static_occ, bfs_persistent<4>, kBlock, 0));
   *base = g_static_base[dev];
   return GRUS_OK;
 }
@@ -676,7 +714,7 @@ extern "C" int grus_bfs_static(uint64_t n, uint64_t m, const uint32_t *offsets,
   cfg.stream = s;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, bfs_persistent, a));
+  GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, bfs_persistent<4>, a));
   if (!stats) return GRUS_OK;
   unsigned char host_ctrl[kCtrlBytes];  // pageable stack copy: no allocation
   GRUS_CUDA_TRY(cudaMemcpyAsync(host_ctrl, ctrl, kCtrlBytes, cudaMemcpyDeviceToHost, s));

@@ -6,7 +6,7 @@
 // lanes idle and a hub of 10^5 edges serialises one warp.  Here a frontier
 // is two work lists, binned when a vertex is enqueued:
 //   queue  : vertex ids of degree 1 .. huge-1
-//   chunks : (v, begin, end) pieces of at most kChunk edges of each vertex of
+//   chunks : (v, begin, end) pieces of at most kChunk (1024) edges of each vertex of
 //            degree >= huge, so hubs spread over every SM
 // and a CTA walks a tile of the queue with three cooperative mappings:
 //   degree >= kCtaTh : the whole CTA strides the list, one vertex at a time
@@ -24,7 +24,7 @@
 
 namespace grus {
 
-constexpr uint32_t kChunk = 4096;  // edges per chunk work item
+constexpr uint32_t kChunk = 1024;  // edges per chunk work item
 constexpr uint32_t kCtaTh = 256;   // CTA-cooperative degree threshold
 
 // Appends vertex v (adjacency [b,e)) to the binned lists of a frontier.
@@ -59,15 +59,11 @@ __device__ __forceinline__ void expand_tile(uint32_t v, uint32_t beg, uint32_t e
                                             uint32_t aux, Visitor &vis) {
   __shared__ uint32_t s_owner, s_src, s_aux, s_beg, s_end;
   const uint32_t lane = lane_id();
-  // CTA-cooperative
-  while (true) {
-    if (threadIdx.x == 0) s_owner = 0xFFFFFFFFu;
+  // CTA-cooperative: one block vote per tile when no source qualifies
+  while (__syncthreads_or(end - beg >= kCtaTh)) {
+    if (end - beg >= kCtaTh) s_owner = threadIdx.x;  // any qualifying thread wins
     __syncthreads();
-    if (end - beg >= kCtaTh) s_owner = threadIdx.x;
-    __syncthreads();
-    const uint32_t owner = s_owner;
-    if (owner == 0xFFFFFFFFu) break;
-    if (threadIdx.x == owner) {
+    if (threadIdx.x == s_owner) {
       s_src = v;
       s_aux = aux;
       s_beg = beg;
@@ -77,7 +73,6 @@ __device__ __forceinline__ void expand_tile(uint32_t v, uint32_t beg, uint32_t e
     __syncthreads();
     const uint32_t cs = s_src, ca = s_aux, cb = s_beg, ce = s_end;
     for (uint32_t x = cb + threadIdx.x; x < ce; x += kBlock) vis.edge(cs, ca, x);
-    __syncthreads();
   }
   // warp-cooperative
   while (true) {

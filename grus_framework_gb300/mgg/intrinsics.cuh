@@ -33,7 +33,7 @@ inline double wtime() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-__global__ inline void dArrayInit(unsigned *ctr, unsigned n, unsigned k = 0) {
+static __global__ void dArrayInit(unsigned *ctr, unsigned n, unsigned k = 0) {
   for (unsigned tid = blockDim.x * blockIdx.x + threadIdx.x; tid < n; tid += blockDim.x * gridDim.x)
     ctr[tid] = k;
 }

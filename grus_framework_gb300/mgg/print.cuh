@@ -18,14 +18,13 @@ template <typename... Args>
 __host__ __device__ __forceinline__ void myprintf(const char *file, int line, const char *fmt,
                                                   Args... args) {
 #if defined(__CUDA_ARCH__)
-  if (TID_1D == 0) {
-    printf("%s:%d GPU: ", file, line);
-    printf(fmt, args...);
-  }
+  if (TID_1D != 0) return;
+  printf("%s:%d GPU: ", file, line);
 #else
   printf("%s:%d HOST: ", file, line);
-  printf(fmt, args...);
 #endif
+  if constexpr (sizeof...(Args) == 0) printf("%s", fmt);
+  else printf(fmt, args...);
 }
 
 template <typename T>

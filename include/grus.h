@@ -104,6 +104,7 @@ typedef struct grus_tuning {
   uint32_t bu_scan;       /* neighbours a pull thread checks before deferring */
   uint32_t timeout_ms;    /* bound on every device-side wait */
   uint32_t sssp_delta;    /* SSSP near/far bucket width (distance units) */
+  uint32_t bu_words;      /* BFS pull levels: bitmap words per warp step (2 or 4) */
 } grus_tuning;
 
 /* ---- library ------------------------------------------------------------- */
@@ -157,6 +158,18 @@ GRUS_API int grus_graph_free(grus_graph *g);
 GRUS_API int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth, grus_stats *stats,
              void *stream);
 
+/* Per-level record of the last grus_bfs call made with stats: level i ends
+ * end_ns after the kernel started; `vertices` were discovered into level i+1
+ * with `edges` out-edges in total; `pull` is 1 for a bottom-up level. */
+typedef struct grus_level_trace {
+  uint64_t end_ns;
+  uint64_t edges;
+  uint32_t vertices;
+  uint32_t pull;
+} grus_level_trace;
+/* Copies up to max_levels records; returns how many (>= 0) or a status. */
+GRUS_API int grus_bfs_trace(grus_graph *g, grus_level_trace *out, int max_levels);
+
 /* Allocation-free BFS.  No counterpart in the reference.  For callers that
  * cannot allocate device memory (a host process that owns the whole device
  * budget through its own pool, or loops where cudaMalloc's device-wide
@@ -165,7 +178,7 @@ GRUS_API int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth, grus_stats *
  * or managed memory; `symmetric` != 0 lets pull levels use the CSR as
  * in-edges, else the BFS runs push-only) with its scratch in a fixed
  * file-scope device array held by every GPU that loads the library (about
- * 9 MB).  Graphs above the limits below are rejected with GRUS_EOVERFLOW.
+ * 10 MB).  Graphs above the limits below are rejected with GRUS_EOVERFLOW.
  * The first call on a device looks the array up (make it before any stream
  * capture).  All calls share the array: calls that overlap on the GPU race.
  * Asynchronous on `stream` unless `stats` is given (then it waits and reports

@@ -86,10 +86,11 @@ def test_bfs_direction_policies(grus, oracle_mod, alpha, beta):
     _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, 5, 12345])
 
 
-@pytest.mark.parametrize("huge,bu_scan,ctas", [(64, 4, 1), (1 << 20, 64, 2), (512, 1, 0)])
-def test_bfs_bins_and_launch_shapes(grus, oracle_mod, huge, bu_scan, ctas):
+@pytest.mark.parametrize("huge,bu_scan,ctas,words", [(64, 4, 1, 2), (1 << 20, 64, 2, 4), (512, 1, 0, 2),
+                                                     (2048, 12, 0, 4)])
+def test_bfs_bins_and_launch_shapes(grus, oracle_mod, huge, bu_scan, ctas, words):
     g = grus.Graph.rmat(14, 32, 9, symmetric=True)
-    g.set_tuning(huge_degree=huge, bu_scan=bu_scan, ctas_per_sm=ctas)
+    g.set_tuning(huge_degree=huge, bu_scan=bu_scan, ctas_per_sm=ctas, bu_words=words)
     _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, 77])
 
 
