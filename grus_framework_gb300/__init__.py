@@ -106,6 +106,7 @@ def _load():
         "grus_bfs": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
         "grus_sssp": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
         "grus_bfs_trace": ([vp, C.POINTER(LevelTrace), i32], i32),
+        "grus_bfs_multi": ([vp, vp, i32, vp, C.POINTER(Stats), vp], i32),
         "grus_cc": ([vp, vp, C.POINTER(Stats), vp], i32),
         "grus_pagerank": ([vp, C.c_float, i32, vp, C.POINTER(Stats), vp], i32),
     }
@@ -322,6 +323,19 @@ def bfs(g: Graph, src: int, out=None, stream=None, stats: bool = False):
     st = Stats() if stats else None
     _check(lib.grus_bfs(g._handle(), src, _ptr(out), C.byref(st) if st is not None else None,
                         _stream(stream)), "grus_bfs")
+    return (out, st.as_dict()) if stats else out
+
+
+def bfs_multi(g: Graph, srcs, out=None, stream=None, stats: bool = False):
+    """Depths from up to 64 sources at once: a (k, n) uint32 array."""
+    srcs = np.ascontiguousarray(srcs, dtype=np.uint32)
+    k = int(srcs.size)
+    if out is None:
+        out = np.empty((k, g.n), np.uint32)
+    st = Stats() if stats else None
+    _check(lib.grus_bfs_multi(g._handle(), _ptr(srcs), k, _ptr(out),
+                              C.byref(st) if st is not None else None, _stream(stream)),
+           "grus_bfs_multi")
     return (out, st.as_dict()) if stats else out
 
 

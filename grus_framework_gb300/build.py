@@ -35,6 +35,7 @@ SOURCES = [
     "sssp.cu",
     "cc.cu",
     "pagerank.cu",
+    "msbfs.cu",
 ]
 
 

@@ -32,8 +32,8 @@
 //     runs push-only.
 //   * direction: Beamer's heuristic -- push->pull when the frontier grows and
 //     m_f > m_u/alpha, pull->push when n_f < n/beta and the frontier shrinks;
-//     the first push level after a pull level reads its sources straight from
-//     the frontier bitmap.
+//     the first push level after a pull level turns the frontier bitmap into
+//     the queue with one atomic per CTA per 256 words.
 // Depths are order-independent (every writer stores level+1), so results are
 // bit-exact against the serial oracle whatever the schedule.
 #include <algorithm>
@@ -184,6 +184,8 @@ struct PushVisitor {
   uint32_t nf;
   unsigned long long mf;
 
+  using aux_t = uint32_t;
+
   __device__ __forceinline__ uint32_t aux(uint32_t) const { return 0u; }
   // Claim dst with one atomicOr on the visited bitmap; the winner writes the
   // depth, marks the next frontier and appends dst to the binned lists.
@@ -304,19 +306,32 @@ __device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32
 }
 
 // First push level after a pull level: its frontier exists only as the
-// bitmap `fcur`, so the sources are the vertex ids whose bit is set, expanded
-// tile by tile with the same binned mappings (no queue conversion, no extra
-// barrier).
-__device__ __forceinline__ void td_from_bitmap(const Args &a, const uint32_t *fcur,
-                                               PushVisitor &vis) {
-  for (uint32_t base = blockIdx.x * kBlock; base < a.n; base += gridDim.x * kBlock) {
-    const uint32_t v = base + threadIdx.x;
-    uint32_t beg = 0, end = 0;
-    if (v < a.n && test_bit(fcur, v)) {
-      beg = __ldg(a.offs + v);
-      end = __ldg(a.offs + v + 1);
+// bitmap `fmap`.  Each CTA owns a contiguous range of words, loads them
+// coalesced and reserves queue space with ONE atomicAdd per 256 words (a
+// block scan of the popcounts places every thread's vertices), so the
+// conversion is a bandwidth pass over n/8 bytes, not a per-vertex atomic
+// storm.  Degrees are not read here: the expansion's CTA mapping takes any
+// degree.
+__device__ __forceinline__ void bitmap_to_queue(const Args &a, const uint32_t *fmap, uint32_t *q,
+                                                uint32_t *qcount) {
+  __shared__ uint32_t s_base;
+  const uint32_t per = (a.W + gridDim.x - 1) / gridDim.x;
+  const uint32_t w0 = blockIdx.x * per, w1 = min(a.W, w0 + per);
+  for (uint32_t base = w0; base < w1; base += kBlock) {
+    const uint32_t w = base + threadIdx.x;
+    uint32_t word = w < w1 ? __ldcg(fmap + w) : 0u;
+    uint32_t total = 0;
+    uint32_t at = block_exclusive_scan<kBlock>(__popc(word), &total);
+    if (threadIdx.x == 0 && total) s_base = atomicAdd(qcount, total);
+    __syncthreads();
+    if (!total) continue;
+    at += s_base;
+    while (word) {
+      const int bit = __ffs(word) - 1;
+      word &= word - 1;
+      if (at < a.queue_cap) q[at] = w * 32 + bit;
+      ++at;
     }
-    expand_tile<kBlock>(v, beg, end, 0u, vis);
   }
 }
 
@@ -361,11 +376,12 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     if (!bu) {
       PushVisitor vis{&a, L + 1, fnext, a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx, 0u, 0ull};
       if (from_pull) {
-        td_from_bitmap(a, fcur, vis);
-      } else {
-        const uint32_t qc = __ldcg(&cur->qcount), cc = __ldcg(&cur->ccount);
-        expand_binned<kBlock>(a.offs, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, vis);
+        bitmap_to_queue(a, fcur, a.queue[L & 1u], &cur->qcount);
+        if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
       }
+      const uint32_t qc = min(__ldcg(&cur->qcount), a.queue_cap);
+      const uint32_t cc = min(__ldcg(&cur->ccount), a.chunk_cap);
+      expand_binned<kBlock>(a.offs, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, vis);
       nf = vis.nf;
       mf = vis.mf;
     } else {

@@ -122,6 +122,7 @@ __global__ void k_collect(const uint32_t *__restrict__ offs, uint32_t *p, uint32
 struct LinkVisitor {
   const uint32_t *offs, *cols;
   uint32_t *p;
+  using aux_t = uint32_t;
   __device__ __forceinline__ uint32_t aux(uint32_t v) const { return __ldg(offs + v) + kSample; }
   __device__ __forceinline__ void edge(uint32_t src, uint32_t first, uint32_t x) {
     if (x < first) return;  // neighbours linked in the sampling rounds
@@ -132,9 +133,11 @@ struct LinkVisitor {
 __global__ void __launch_bounds__(kBlock) k_link_rest(const uint32_t *__restrict__ offs,
                                                       const uint32_t *__restrict__ cols,
                                                       uint32_t *p, const Ctl *ctl,
-                                                      const uint32_t *queue, const uint4 *chunks) {
+                                                      const uint32_t *queue, uint32_t qcap,
+                                                      const uint4 *chunks, uint32_t ccap) {
   LinkVisitor vis{offs, cols, p};
-  expand_binned<kBlock>(offs, queue, __ldcg(&ctl->qcount), chunks, __ldcg(&ctl->ccount), vis);
+  expand_binned<kBlock>(offs, queue, min(__ldcg(&ctl->qcount), qcap), chunks,
+                        min(__ldcg(&ctl->ccount), ccap), vis);
 }
 
 struct Workspace {
@@ -216,7 +219,7 @@ extern "C" int grus_cc(grus_graph *g, uint32_t *label, grus_stats *stats, void *
   k_collect<<<grid, kBlock, 0, s>>>(g->csr.offs, w->parent, n, w->ctl, w->queue, w->chunks,
                                     w->ccap, huge, (g->flags & GRUS_GRAPH_SYMMETRIC) != 0);
   k_link_rest<<<sms * std::max(occ, 1), kBlock, 0, s>>>(g->csr.offs, g->csr.cols, w->parent,
-                                                          w->ctl, w->queue, w->chunks);
+                                                          w->ctl, w->queue, n, w->chunks, w->ccap);
   uint32_t *dst = dev_out ? label : w->parent;
   k_compress<<<grid, kBlock, 0, s>>>(w->parent, dev_out ? label : nullptr, n);
   GRUS_CUDA_TRY(cudaGetLastError());

@@ -119,4 +119,36 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
   return t;
 }
 
+// Block-wide exclusive scan of one value per thread; *total gets the sum.
+// Must be called by every thread of the block.
+template <int kBlock>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t s_warp[kBlock / 32];
+  __shared__ uint32_t s_total;
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((int)lane >= o) incl += t;
+  }
+  __syncthreads();
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < kBlock / 32 ? s_warp[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+      if ((int)lane >= o) wi += t;
+    }
+    if (lane < kBlock / 32) s_warp[lane] = wi - w;
+    if (lane == 31) s_total = wi;
+  }
+  __syncthreads();
+  *total = s_total;
+  return s_warp[warp] + incl - v;
+}
+
 }  // namespace grus

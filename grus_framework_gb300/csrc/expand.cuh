@@ -16,8 +16,9 @@
 //                      owner is found by a shuffle binary search over the
 //                      inclusive degree scan.
 // Column loads are coalesced in every mapping.  A Visitor supplies
-//   uint32_t aux(uint32_t v)                   per-source value, loaded once
-//   void edge(uint32_t src, uint32_t aux, uint32_t x)   work on edge index x
+//   using aux_t = ...;                         type of the per-source value
+//   aux_t aux(uint32_t v)                      per-source value, loaded once
+//   void edge(uint32_t src, aux_t aux, uint32_t x)   work on edge index x
 #pragma once
 
 #include "device_util.cuh"
@@ -56,8 +57,10 @@ __device__ __forceinline__ bool push_binned(uint32_t v, uint32_t b, uint32_t e,
 // Must be called by every thread of the CTA.
 template <int kBlock, class Visitor>
 __device__ __forceinline__ void expand_tile(uint32_t v, uint32_t beg, uint32_t end,
-                                            uint32_t aux, Visitor &vis) {
-  __shared__ uint32_t s_owner, s_src, s_aux, s_beg, s_end;
+                                            typename Visitor::aux_t aux, Visitor &vis) {
+  using A = typename Visitor::aux_t;
+  __shared__ uint32_t s_owner, s_src, s_beg, s_end;
+  __shared__ A s_aux;
   const uint32_t lane = lane_id();
   // CTA-cooperative: one block vote per tile when no source qualifies
   while (__syncthreads_or(end - beg >= kCtaTh)) {
@@ -71,7 +74,8 @@ __device__ __forceinline__ void expand_tile(uint32_t v, uint32_t beg, uint32_t e
       beg = end;
     }
     __syncthreads();
-    const uint32_t cs = s_src, ca = s_aux, cb = s_beg, ce = s_end;
+    const uint32_t cs = s_src, cb = s_beg, ce = s_end;
+    const A ca = s_aux;
     for (uint32_t x = cb + threadIdx.x; x < ce; x += kBlock) vis.edge(cs, ca, x);
   }
   // warp-cooperative
@@ -80,7 +84,7 @@ __device__ __forceinline__ void expand_tile(uint32_t v, uint32_t beg, uint32_t e
     if (!ball) break;
     const int leader = __ffs(ball) - 1;
     const uint32_t ws = __shfl_sync(0xffffffffu, v, leader);
-    const uint32_t wa = __shfl_sync(0xffffffffu, aux, leader);
+    const A wa = __shfl_sync(0xffffffffu, aux, leader);
     const uint32_t wb = __shfl_sync(0xffffffffu, beg, leader);
     const uint32_t we = __shfl_sync(0xffffffffu, end, leader);
     if ((int)lane == leader) beg = end;
@@ -104,7 +108,7 @@ __device__ __forceinline__ void expand_tile(uint32_t v, uint32_t beg, uint32_t e
       if (pv <= k) j += step;
     }
     const uint32_t os = __shfl_sync(0xffffffffu, v, j);
-    const uint32_t oa = __shfl_sync(0xffffffffu, aux, j);
+    const A oa = __shfl_sync(0xffffffffu, aux, j);
     const uint32_t ob = __shfl_sync(0xffffffffu, beg, j);
     const uint32_t oi = __shfl_sync(0xffffffffu, incl, j);
     const uint32_t od = __shfl_sync(0xffffffffu, deg, j);
@@ -117,7 +121,7 @@ template <int kBlock, class Visitor>
 __device__ __forceinline__ void expand_chunks(const uint4 *ccur, uint32_t ccount, Visitor &vis) {
   for (uint32_t c = blockIdx.x; c < ccount; c += gridDim.x) {
     const uint4 ch = __ldcg(ccur + c);
-    const uint32_t a = vis.aux(ch.x);
+    const typename Visitor::aux_t a = vis.aux(ch.x);
     for (uint32_t x = ch.y + threadIdx.x; x < ch.z; x += kBlock) vis.edge(ch.x, a, x);
   }
 }
@@ -131,7 +135,8 @@ __device__ __forceinline__ void expand_binned(const uint32_t *__restrict__ offs,
                                               Visitor &vis) {
   for (uint32_t base = blockIdx.x * kBlock; base < qcount; base += gridDim.x * kBlock) {
     const uint32_t i = base + threadIdx.x;
-    uint32_t v = 0, beg = 0, end = 0, aux = 0;
+    uint32_t v = 0, beg = 0, end = 0;
+    typename Visitor::aux_t aux{};
     if (i < qcount) {
       v = __ldcg(qcur + i);
       beg = __ldg(offs + v);

@@ -158,6 +158,8 @@ struct RelaxVisitor {
   Slot *nx;
   unsigned long long visits;
 
+  using aux_t = uint32_t;
+
   __device__ __forceinline__ uint32_t aux(uint32_t v) const { return __ldcg(a->dist + v); }
   __device__ __forceinline__ void edge(uint32_t, uint32_t du, uint32_t x) {
     ++visits;
@@ -207,7 +209,8 @@ __global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
     uint32_t *inq_clr = a.inq[(L + 2) % 3];
     for (uint32_t i = gtid; i < a.W; i += nthreads) inq_clr[i] = 0u;
     if (gtid < sizeof(Slot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[gtid] = 0u;
-    const uint32_t qc = __ldcg(&cur->qcount), cc = __ldcg(&cur->ccount);
+    const uint32_t qc = min(__ldcg(&cur->qcount), a.queue_cap);
+    const uint32_t cc = min(__ldcg(&cur->ccount), a.chunk_cap);
     RelaxVisitor vis{&a, T, inq_next, a.queue[(L + 1) & 1u], a.far[fsel],
                      &a.farctl->count[fsel], a.chunks[(L + 1) & 1u], nx, 0ull};
     expand_binned<kBlock>(a.offs, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, vis);
@@ -219,7 +222,7 @@ __global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
     bool done = false;
     // near frontier empty: advance the threshold and split the far pile
     while (__ldcg(&nx->qcount) + __ldcg(&nx->ccount) == 0) {
-      const uint32_t fc = __ldcg(&a.farctl->count[fsel]);
+      const uint32_t fc = min(__ldcg(&a.farctl->count[fsel]), a.queue_cap);
       if (fc == 0) {
         done = true;
         break;

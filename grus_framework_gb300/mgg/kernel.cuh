@@ -72,6 +72,7 @@ struct ToFlag {  // generator(bool, char *flag, dst)
   const vtx_t *adjncy;
   char *flag;
   J job;
+  using aux_t = uint32_t;
   __device__ __forceinline__ uint32_t aux(uint32_t) const { return 0u; }
   __device__ __forceinline__ void edge(uint32_t src, uint32_t, uint32_t x) {
     U updater;
@@ -86,6 +87,7 @@ struct ToFlagFinished {  // generator(bool, char *flag, dst, char *finished)
   const vtx_t *adjncy;
   char *flag, *finished;
   J job;
+  using aux_t = uint32_t;
   __device__ __forceinline__ uint32_t aux(uint32_t) const { return 0u; }
   __device__ __forceinline__ void edge(uint32_t src, uint32_t, uint32_t x) {
     U updater;
@@ -100,6 +102,7 @@ struct ToWorklist {  // generator(bool, Worklist, dst)
   const vtx_t *adjncy;
   worklist::Worklist wl;
   J job;
+  using aux_t = uint32_t;
   __device__ __forceinline__ uint32_t aux(uint32_t) const { return 0u; }
   __device__ __forceinline__ void edge(uint32_t src, uint32_t, uint32_t x) {
     U updater;
@@ -115,6 +118,7 @@ struct PullFromFlag {  // the owner is dst; in-edge x brings src
   const char *flag1;
   char *flag2, *finished;
   J job;
+  using aux_t = uint32_t;
   __device__ __forceinline__ uint32_t aux(uint32_t) const { return 0u; }
   __device__ __forceinline__ void edge(uint32_t dst, uint32_t, uint32_t x) {
     const vtx_t src = adjncy[x];
@@ -130,8 +134,8 @@ struct PullFromFlag {  // the owner is dst; in-edge x brings src
 template <class Vis>
 __global__ void __launch_bounds__(kBlock)
     expand_queue(const vtx_t *__restrict__ xadj, const vtx_t *queue, const vtx_t *qcount_d,
-                 uint4 *chunks, vtx_t *ccount, uint32_t ccap, Vis vis) {
-  const vtx_t qcount = *qcount_d;
+                 vtx_t qcap, uint4 *chunks, vtx_t *ccount, uint32_t ccap, Vis vis) {
+  const vtx_t qcount = min(*qcount_d, qcap);
   for (uint32_t base = blockIdx.x * kBlock; base < qcount; base += gridDim.x * kBlock) {
     const uint32_t i = base + threadIdx.x;
     vtx_t v = 0, beg = 0, end = 0;
@@ -164,8 +168,8 @@ __global__ void __launch_bounds__(kBlock)
 
 template <class Vis>
 __global__ void __launch_bounds__(kBlock)
-    expand_pieces(const uint4 *chunks, const vtx_t *ccount, Vis vis) {
-  grus::expand_chunks<kBlock>(chunks, *ccount, vis);
+    expand_pieces(const uint4 *chunks, const vtx_t *ccount, uint32_t ccap, Vis vis) {
+  grus::expand_chunks<kBlock>(chunks, min(*ccount, ccap), vis);
 }
 
 struct ByteActive {
@@ -183,14 +187,14 @@ struct SelectorActive {
 };
 
 template <class Vis>
-void run_queue(const vtx_t *xadj, uint64_t m, frontier::FrontierAux *aux, const vtx_t *queue,
-               const vtx_t *qcount_d, vtx_t qcount_h, const Vis &vis) {
+void run_queue(const vtx_t *xadj, uint64_t m, frontier::FrontierAux *aux,
+               const worklist::Worklist &wl, vtx_t qcount_h, const Vis &vis) {
   if (qcount_h == 0) return;
   aux->ensure(m, kHuge, grus::kChunk);
   H_ERR(cudaMemsetAsync(aux->ccount, 0, sizeof(vtx_t), NULL));
-  expand_queue<Vis><<<grid_for(qcount_h), kBlock>>>(xadj, queue, qcount_d, aux->chunks, aux->ccount,
-                                                    aux->chunk_cap, vis);
-  expand_pieces<Vis><<<sm_count() * 2, kBlock>>>(aux->chunks, aux->ccount, vis);
+  expand_queue<Vis><<<grid_for(qcount_h), kBlock>>>(xadj, wl.data, wl.count, wl.capacity,
+                                                    aux->chunks, aux->ccount, aux->chunk_cap, vis);
+  expand_pieces<Vis><<<sm_count() * 2, kBlock>>>(aux->chunks, aux->ccount, aux->chunk_cap, vis);
 }
 
 template <class Active, class Vis>
@@ -201,7 +205,7 @@ void run_range(const vtx_t *xadj, uint64_t m, frontier::FrontierAux *aux, vtx_t 
   H_ERR(cudaMemsetAsync(aux->ccount, 0, sizeof(vtx_t), NULL));
   expand_range<Active, Vis><<<grid_for(n), kBlock>>>(xadj, n, active, aux->chunks, aux->ccount,
                                                      aux->chunk_cap, vis);
-  expand_pieces<Vis><<<sm_count() * 2, kBlock>>>(aux->chunks, aux->ccount, vis);
+  expand_pieces<Vis><<<sm_count() * 2, kBlock>>>(aux->chunks, aux->ccount, aux->chunk_cap, vis);
 }
 
 }  // namespace detail
@@ -231,8 +235,10 @@ class kernel<graph_t, frontier::Frontier<WL>, updater_t, generator_t, job_t> {
  public:
   void operator()(graph_t G, frontier::Frontier<WL> F, job_t job) {
     job.prepare();
+    // a generator may append a vertex once per in-edge: room for every edge
+    F.wl_n->grow(std::max<uint64_t>(G.numNode, G.numEdge));
     detail::ToWorklist<updater_t, generator_t, job_t> vis{G.adjncy, *F.wl_n, job};
-    detail::run_queue(G.xadj, G.numEdge, F.aux, F.wl_c->data, F.wl_c->count, F.get_work_size_h(), vis);
+    detail::run_queue(G.xadj, G.numEdge, F.aux, *F.wl_c, F.get_work_size_h(), vis);
   }
 };
 
@@ -242,7 +248,7 @@ class kernel<graph_t, frontier::Frontier<BDF>, updater_t, generator_t, job_t> {
   void operator()(graph_t G, frontier::Frontier<BDF> F, job_t job) {
     job.prepare();
     detail::ToFlag<updater_t, generator_t, job_t> vis{G.adjncy, F.flag2, job};
-    detail::run_queue(G.xadj, G.numEdge, F.aux, F.wl1.data, F.wl1.count, F.get_work_size_h(), vis);
+    detail::run_queue(G.xadj, G.numEdge, F.aux, F.wl1, F.get_work_size_h(), vis);
   }
 };
 
@@ -263,8 +269,9 @@ class kernel<graph_t, frontier::Frontier<BDF_AUTO>, updater_t, generator_t, job_
     job.prepare();
     switch (F.current_f) {
       case WL: {
+        F.wl_n->grow(std::max<uint64_t>(G.numNode, G.numEdge));
         detail::ToWorklist<updater_t, generator_t, job_t> vis{G.adjncy, *F.wl_n, job};
-        detail::run_queue(G.xadj, G.numEdge, F.aux, F.wl_c->data, F.wl_c->count, F.wl_sz, vis);
+        detail::run_queue(G.xadj, G.numEdge, F.aux, *F.wl_c, F.wl_sz, vis);
         break;
       }
       case BITMAP: {
@@ -274,7 +281,7 @@ class kernel<graph_t, frontier::Frontier<BDF_AUTO>, updater_t, generator_t, job_
       }
       default: {
         detail::ToFlag<updater_t, generator_t, job_t> vis{G.adjncy, F.flag2, job};
-        detail::run_queue(G.xadj, G.numEdge, F.aux, F.wl_c->data, F.wl_c->count, F.wl_sz, vis);
+        detail::run_queue(G.xadj, G.numEdge, F.aux, *F.wl_c, F.wl_sz, vis);
         break;
       }
     }

@@ -28,6 +28,7 @@ struct SubgraphToFlag {
   const vtx_t *edges;
   char *flag;
   J job;
+  using aux_t = uint32_t;
   __device__ __forceinline__ uint32_t aux(uint32_t) const { return 0u; }
   __device__ __forceinline__ void edge(uint32_t src, uint32_t, uint32_t x) {
     U updater;
@@ -40,9 +41,9 @@ struct SubgraphToFlag {
 // Queue of global ids; rows come from the subgraph through its lookup.
 template <class Vis>
 __global__ void __launch_bounds__(kBlock)
-    expand_subgraph(const vtx_t *queue, const vtx_t *qcount_d, const vtx_t *lookup,
+    expand_subgraph(const vtx_t *queue, const vtx_t *qcount_d, vtx_t qcap, const vtx_t *lookup,
                     const vtx_t *vtx_ptr, Vis vis) {
-  const vtx_t qcount = *qcount_d;
+  const vtx_t qcount = min(*qcount_d, qcap);
   for (uint32_t base = blockIdx.x * kBlock; base < qcount; base += gridDim.x * kBlock) {
     const uint32_t i = base + threadIdx.x;
     vtx_t v = 0, beg = 0, end = 0;
@@ -74,14 +75,14 @@ class kernel_2s<graph_t, Subgraph<NORMAL>, frontier::Frontier_2S<BDF>, updater_t
     if (F.wl_sz_local) {
       detail::SubgraphToFlag<updater_t, generator_t, job_t> vis{SG1.edges, F.flag2, job};
       detail::expand_subgraph<<<detail::grid_for(F.wl_sz_local), detail::kBlock>>>(
-          F.wl_local->data, F.wl_local->count, SG1.lookup_buffer, SG1.vtx_ptr, vis);
+          F.wl_local->data, F.wl_local->count, F.wl_local->capacity, SG1.lookup_buffer, SG1.vtx_ptr, vis);
     }
     SG1.clean();
     SG2.build(G, *F.wl_remote);
     if (F.wl_sz_remote) {
       detail::SubgraphToFlag<updater_t, generator_t, job_t> vis{SG2.edges, F.flag2, job};
       detail::expand_subgraph<<<detail::grid_for(F.wl_sz_remote), detail::kBlock>>>(
-          F.wl_remote->data, F.wl_remote->count, SG2.lookup_buffer, SG2.vtx_ptr, vis);
+          F.wl_remote->data, F.wl_remote->count, F.wl_remote->capacity, SG2.lookup_buffer, SG2.vtx_ptr, vis);
     }
   }
 };

@@ -35,15 +35,29 @@ void Worklist::initFull(vtx_t n) {
   c_count = n;
 }
 
+// The device count keeps growing when appends overflow (they are dropped, not
+// written), so every host read is clamped to the capacity.
 vtx_t Worklist::get_sz() {
   H_ERR(cudaMemcpy(&c_count, count, sizeof(vtx_t), cudaMemcpyDeviceToHost));
+  if (c_count > capacity) c_count = capacity;
   return c_count;
 }
 
 vtx_t Worklist::get_sz(cudaStream_t stream) {
   H_ERR(cudaMemcpyAsync(&c_count, count, sizeof(vtx_t), cudaMemcpyDeviceToHost, stream));
   H_ERR(cudaStreamSynchronize(stream));
+  if (c_count > capacity) c_count = capacity;
   return c_count;
+}
+
+void Worklist::grow(size_t cap) {
+  if (cap <= capacity) return;
+  vtx_t *fresh = nullptr;
+  H_ERR(cudaMalloc(&fresh, cap * sizeof(vtx_t)));
+  H_ERR(cudaMemcpy(fresh, data, (size_t)capacity * sizeof(vtx_t), cudaMemcpyDeviceToDevice));
+  H_ERR(cudaFree(data));
+  data = fresh;
+  capacity = (vtx_t)cap;
 }
 
 void Worklist::reset() {
@@ -73,7 +87,7 @@ __global__ void flag_to_wl(Worklist wl, char *flag1, vtx_t size) {
 // Bounds are the queue length (the reference bounds by n, src/worklist.cu:94-100).
 __global__ void wl_to_flag(Worklist wl, char *flag1, vtx_t size) {
   const size_t tid = blockDim.x * (size_t)blockIdx.x + threadIdx.x;
-  const vtx_t len = *wl.count;
+  const vtx_t len = min(*wl.count, wl.capacity);
   if (tid < size && tid < len) flag1[wl.data[tid]] = 1;
 }
 

@@ -37,6 +37,8 @@ class Worklist {
   __host__ void reset();
   __host__ void add_item(vtx_t item, cudaStream_t stream);
   __host__ void creset() { c_count = 0; }
+  // Enlarges the buffer (keeping its contents) to at least `cap` items.
+  __host__ void grow(size_t cap);
 
   __device__ __forceinline__ void append(const vtx_t &item) {
     const vtx_t at = atomicAdd((vtx_t *)count, 1u);
@@ -52,7 +54,7 @@ class Worklist {
   }
   __device__ __forceinline__ void reset_d() const { *count = 0; }
   __device__ __forceinline__ vtx_t read(vtx_t i) const { return data[i]; }
-  __device__ __forceinline__ vtx_t size() const { return *count; }
+  __device__ __forceinline__ vtx_t size() const { return min(*count, capacity); }
   __device__ __forceinline__ void assign(vtx_t i, vtx_t t) const { data[i] = t; }
 };
 

@@ -158,6 +158,16 @@ GRUS_API int grus_graph_free(grus_graph *g);
 GRUS_API int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth, grus_stats *stats,
              void *stream);
 
+/* Multi-source BFS: k <= 64 sources advance together in one persistent
+ * launch, one bit per source in a 64-bit word per vertex.  `srcs` (host or
+ * device, k entries) may repeat vertices; `depths` holds k*n uint32,
+ * source-major (depths[i*n + v] = depth of v from srcs[i], GRUS_INFINIT if
+ * unreached).  The reference answers one source per run of its BFS sample
+ * (samples/bfs/bfs.cu:135-173).  stats->vertices_reached / edges_reached are
+ * summed over the sources. */
+GRUS_API int grus_bfs_multi(grus_graph *g, const uint32_t *srcs, int k, uint32_t *depths,
+                   grus_stats *stats, void *stream);
+
 /* Per-level record of the last grus_bfs call made with stats: level i ends
  * end_ns after the kernel started; `vertices` were discovered into level i+1
  * with `edges` out-edges in total; `pull` is 1 for a bottom-up level. */

@@ -1,0 +1,85 @@
+"""GPU: 64-source BFS (one persistent launch, 64-bit frontier words) against
+k independent oracle BFS runs -- bit-exact, row per source."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+INF = 4294967294
+
+
+def host_csr(g):
+    import oracle
+    offs, cols, wts = g.copy_csr()
+    return oracle.CSR(offs, cols, wts)
+
+
+def check(grus, oracle_mod, g, srcs):
+    h = host_csr(g)
+    d, st = grus.bfs_multi(g, srcs, stats=True)
+    ref = oracle_mod.bfs_multi(h, srcs)
+    assert d.shape == ref.shape
+    bad = np.count_nonzero(d != ref)
+    assert bad == 0, f"{bad} mismatching (source, vertex) depths"
+    assert st["vertices_reached"] == int(np.count_nonzero(ref != INF))
+    return st
+
+
+@pytest.mark.parametrize("k", [1, 7, 33, 64])
+def test_msbfs_rmat_symmetric(grus, oracle_mod, k):
+    g = grus.Graph.rmat(14, 16, 4, symmetric=True)
+    rng = np.random.default_rng(k)
+    deg = np.diff(host_csr(g).offs.astype(np.int64))
+    cand = np.flatnonzero(deg > 0)
+    srcs = rng.choice(cand, size=k, replace=True).astype(np.uint32)
+    st = check(grus, oracle_mod, g, srcs)
+    assert st["levels"] >= 2
+
+
+def test_msbfs_repeated_and_isolated_sources(grus, oracle_mod):
+    g = grus.Graph.rmat(12, 8, 2, symmetric=True)
+    deg = np.diff(host_csr(g).offs.astype(np.int64))
+    iso = int(np.flatnonzero(deg == 0)[0])
+    hub = g.max_degree_vertex
+    check(grus, oracle_mod, g, np.array([hub, hub, iso, 5, hub, iso], np.uint32))
+
+
+@pytest.mark.parametrize("alpha", [1e9, 1e-3])
+def test_msbfs_push_only_and_pull_heavy(grus, oracle_mod, alpha):
+    g = grus.Graph.rmat(13, 16, 9, symmetric=True)
+    g.set_tuning(alpha=alpha)
+    srcs = np.arange(0, 64 * 97, 97, dtype=np.uint32) % g.n
+    check(grus, oracle_mod, g, srcs)
+
+
+def test_msbfs_directed_with_and_without_csc(grus, oracle_mod):
+    g = grus.Graph.rmat(12, 16, 6, symmetric=False)
+    srcs = np.arange(64, dtype=np.uint32) * 61 % g.n
+    check(grus, oracle_mod, g, srcs)
+    g.build_csc()
+    g.set_tuning(alpha=1e-3)
+    check(grus, oracle_mod, g, srcs)
+
+
+def test_msbfs_grid(grus, oracle_mod):
+    g = grus.Graph.grid2d(64, 90)
+    srcs = np.array([0, 91, 5759, 1000, 2500], np.uint32)
+    check(grus, oracle_mod, g, srcs)
+
+
+def test_msbfs_device_output(grus, oracle_mod):
+    torch = pytest.importorskip("torch")
+    g = grus.Graph.rmat(11, 16, 8, symmetric=True)
+    srcs = np.arange(64, dtype=np.uint32)
+    out = torch.empty((64, g.n), dtype=torch.int32, device="cuda")
+    grus.bfs_multi(g, srcs, out=out)
+    torch.cuda.synchronize()
+    ref = oracle_mod.bfs_multi(host_csr(g), srcs)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), ref)
+
+
+def test_msbfs_rejects_bad_arguments(grus):
+    g = grus.Graph.rmat(8, 4, 1)
+    with pytest.raises(grus.GrusError):
+        grus.bfs_multi(g, np.zeros(65, np.uint32))
+    with pytest.raises(grus.GrusError):
+        grus.bfs_multi(g, np.array([g.n], np.uint32))
