@@ -26,6 +26,7 @@ OK, ENOENT, EIO, ENOMEM, EBUSY, ENODEV, EINVAL, EOVERFLOW, ETIMEDOUT, ECUDA = (
 MEM_DEVICE, MEM_MANAGED = 0, 1
 GRAPH_SYMMETRIC, GRAPH_WEIGHTED = 1, 2
 GEN_SYMMETRIC, GEN_WEIGHTED, GEN_RELABEL = 1, 2, 4
+ALGO_BFS, ALGO_SSSP = 0, 1
 
 
 class GrusError(RuntimeError):
@@ -70,6 +71,33 @@ class LevelTrace(C.Structure):
                 ("pull", C.c_uint32)]
 
 
+class Query(C.Structure):
+    _fields_ = [("graph", C.c_uint32), ("algo", C.c_uint32), ("src", C.c_uint32),
+                ("reserved", C.c_uint32), ("out_offset", C.c_uint64)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("cluster_size", C.c_uint32), ("workers", C.c_uint32),
+                ("huge_degree", C.c_uint32), ("sssp_delta", C.c_uint32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("cluster_size", C.c_uint32),
+                ("hbm_reserve_bytes", C.c_uint64), ("sssp_delta", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("status", C.c_int32), ("reserved", C.c_uint32),
+                ("latency_us", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
+                ("pending", C.c_uint64), ("rejected", C.c_uint64), ("slots", C.c_uint32),
+                ("slots_ready", C.c_uint32)]
+
+
 class Tuning(C.Structure):
     _fields_ = [
         ("alpha", C.c_float), ("beta", C.c_float), ("ctas_per_sm", C.c_uint32),
@@ -107,6 +135,15 @@ def _load():
         "grus_sssp": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
         "grus_bfs_trace": ([vp, C.POINTER(LevelTrace), i32], i32),
         "grus_bfs_multi": ([vp, vp, i32, vp, C.POINTER(Stats), vp], i32),
+        "grus_batch_create": ([C.POINTER(vp), i32, C.POINTER(BatchConfig), PG], i32),
+        "grus_batch_run": ([vp, C.POINTER(Query), i32, vp, i32, C.POINTER(Stats), vp], i32),
+        "grus_batch_get_info": ([vp, C.POINTER(BatchConfig)], i32),
+        "grus_batch_free": ([vp], i32),
+        "grus_server_create": ([C.POINTER(vp), i32, C.POINTER(ServerConfig), PG], i32),
+        "grus_server_submit": ([vp, u32, u32, u32, vp, u64], i32),
+        "grus_server_poll": ([vp, C.POINTER(Completion), i32, i32], i32),
+        "grus_server_get_stats": ([vp, C.POINTER(ServerStats)], i32),
+        "grus_server_destroy": ([vp], i32),
         "grus_cc": ([vp, vp, C.POINTER(Stats), vp], i32),
         "grus_pagerank": ([vp, C.c_float, i32, vp, C.POINTER(Stats), vp], i32),
     }
@@ -376,3 +413,98 @@ def pagerank(g: Graph, damping: float = 0.85, iters: int = 20, out=None, stream=
                              C.byref(st) if st is not None else None, _stream(stream)),
            "grus_pagerank")
     return (out, st.as_dict()) if stats else out
+
+
+def _graph_array(graphs):
+    arr = (C.c_void_p * len(graphs))(*[g._handle().value for g in graphs])
+    return arr
+
+
+class Batch:
+    """Many BFS / SSSP queries over several resident graphs in one launch
+    (cluster workers, include/grus.h grus_batch_*)."""
+
+    def __init__(self, graphs, cluster_size=0, workers=0, huge_degree=0, sssp_delta=0):
+        self.graphs = list(graphs)
+        cfg = BatchConfig(cluster_size, workers, huge_degree, sssp_delta)
+        h = C.c_void_p()
+        _check(lib.grus_batch_create(_graph_array(self.graphs), len(self.graphs), C.byref(cfg),
+                                     C.byref(h)), "grus_batch_create")
+        self._h = h
+
+    def layout(self, queries):
+        """Output offsets of a list of (graph, algo, src) and the total size."""
+        offs, at = [], 0
+        for gi, _, _ in queries:
+            offs.append(at)
+            at += self.graphs[gi].n
+        return offs, at
+
+    def run(self, queries, out, offsets=None, use_graph=False, stream=None, stats=False):
+        """queries: list of (graph_index, algo, src); out: device buffer
+        (uint32/int32 tensor or pointer) holding every result back to back."""
+        if offsets is None:
+            offsets, _ = self.layout(queries)
+        arr = (Query * len(queries))()
+        for i, ((gi, algo, src), off) in enumerate(zip(queries, offsets)):
+            arr[i] = Query(gi, algo, src, 0, off)
+        st = Stats() if stats else None
+        _check(lib.grus_batch_run(self._h, arr, len(queries), _ptr(out), int(bool(use_graph)),
+                                  C.byref(st) if st is not None else None, _stream(stream)),
+               "grus_batch_run")
+        return st.as_dict() if stats else None
+
+    def info(self):
+        cfg = BatchConfig()
+        _check(lib.grus_batch_get_info(self._h, C.byref(cfg)), "grus_batch_get_info")
+        return {k: getattr(cfg, k) for k, _ in cfg._fields_}
+
+    def free(self):
+        if self._h and self._h.value:
+            lib.grus_batch_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Server:
+    """Query server over resident graphs (include/grus.h grus_server_*)."""
+
+    def __init__(self, graphs, slots=16, cluster_size=8, hbm_reserve_bytes=0, sssp_delta=0):
+        self.graphs = list(graphs)
+        cfg = ServerConfig(slots, cluster_size, hbm_reserve_bytes, sssp_delta, 0)
+        h = C.c_void_p()
+        _check(lib.grus_server_create(_graph_array(self.graphs), len(self.graphs), C.byref(cfg),
+                                      C.byref(h)), "grus_server_create")
+        self._h = h
+
+    def submit(self, graph, algo, src, out, tag):
+        _check(lib.grus_server_submit(self._h, graph, algo, src, _ptr(out), tag),
+               "grus_server_submit")
+
+    def poll(self, max_items=256, wait_ms=0):
+        buf = (Completion * max_items)()
+        k = lib.grus_server_poll(self._h, buf, max_items, wait_ms)
+        if k < 0:
+            _check(k, "grus_server_poll")
+        return [(buf[i].tag, buf[i].status, buf[i].latency_us) for i in range(k)]
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib.grus_server_get_stats(self._h, C.byref(st)), "grus_server_get_stats")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if self._h and self._h.value:
+            lib.grus_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

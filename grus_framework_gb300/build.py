@@ -36,6 +36,8 @@ SOURCES = [
     "cc.cu",
     "pagerank.cu",
     "msbfs.cu",
+    "batch.cu",
+    "serve.cu",
 ]
 
 

@@ -117,13 +117,21 @@ __device__ __forceinline__ void expand_tile(uint32_t v, uint32_t beg, uint32_t e
 }
 
 // Chunk list: one (v, begin, end) piece per CTA, the whole CTA strides it.
+// `part`/`parts` name this CTA among the CTAs sharing the work (the grid, or
+// one thread-block cluster).
 template <int kBlock, class Visitor>
-__device__ __forceinline__ void expand_chunks(const uint4 *ccur, uint32_t ccount, Visitor &vis) {
-  for (uint32_t c = blockIdx.x; c < ccount; c += gridDim.x) {
+__device__ __forceinline__ void expand_chunks(const uint4 *ccur, uint32_t ccount, Visitor &vis,
+                                              uint32_t part, uint32_t parts) {
+  for (uint32_t c = part; c < ccount; c += parts) {
     const uint4 ch = __ldcg(ccur + c);
     const typename Visitor::aux_t a = vis.aux(ch.x);
     for (uint32_t x = ch.y + threadIdx.x; x < ch.z; x += kBlock) vis.edge(ch.x, a, x);
   }
+}
+
+template <int kBlock, class Visitor>
+__device__ __forceinline__ void expand_chunks(const uint4 *ccur, uint32_t ccount, Visitor &vis) {
+  expand_chunks<kBlock>(ccur, ccount, vis, blockIdx.x, gridDim.x);
 }
 
 // Expands the queue tile-by-tile, then the chunk list.  Must be called by
@@ -132,8 +140,8 @@ template <int kBlock, class Visitor>
 __device__ __forceinline__ void expand_binned(const uint32_t *__restrict__ offs,
                                               const uint32_t *qcur, uint32_t qcount,
                                               const uint4 *ccur, uint32_t ccount,
-                                              Visitor &vis) {
-  for (uint32_t base = blockIdx.x * kBlock; base < qcount; base += gridDim.x * kBlock) {
+                                              Visitor &vis, uint32_t part, uint32_t parts) {
+  for (uint32_t base = part * kBlock; base < qcount; base += parts * kBlock) {
     const uint32_t i = base + threadIdx.x;
     uint32_t v = 0, beg = 0, end = 0;
     typename Visitor::aux_t aux{};
@@ -145,7 +153,15 @@ __device__ __forceinline__ void expand_binned(const uint32_t *__restrict__ offs,
     }
     expand_tile<kBlock>(v, beg, end, aux, vis);
   }
-  expand_chunks<kBlock>(ccur, ccount, vis);
+  expand_chunks<kBlock>(ccur, ccount, vis, part, parts);
+}
+
+template <int kBlock, class Visitor>
+__device__ __forceinline__ void expand_binned(const uint32_t *__restrict__ offs,
+                                              const uint32_t *qcur, uint32_t qcount,
+                                              const uint4 *ccur, uint32_t ccount,
+                                              Visitor &vis) {
+  expand_binned<kBlock>(offs, qcur, qcount, ccur, ccount, vis, blockIdx.x, gridDim.x);
 }
 
 }  // namespace grus

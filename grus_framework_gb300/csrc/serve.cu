@@ -1,0 +1,320 @@
+// serve.cu -- a query server over device-resident graphs (continuous batching).
+//
+// Requests (graph, BFS|SSSP, source, device output) are queued by
+// grus_server_submit from any host thread.  A scheduler thread admits them
+// into worker slots: a slot is one cluster worker of the batch engine
+// (batch.cu) with its own per-query device state and CUDA stream.  A slot's
+// state is allocated the first time it is used, and only if free HBM
+// (cudaMemGetInfo) covers it plus a reserve -- admission by free HBM.  Each
+// admitted query is one single-worker launch on its slot's stream, so queries
+// that arrive while others run start as soon as a slot is free and overlap on
+// the device.  Completion is observed with an event per slot; latency is
+// completion time minus submission time on the host clock.
+// The reference has no serving path (one query per process run).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "batch.cuh"
+#include "grus_internal.cuh"
+
+namespace grus {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  uint64_t tag;
+  uint32_t graph, algo, src;
+  uint32_t *out;
+  Clock::time_point t_submit;
+};
+
+struct Slot {
+  BatchState state;        // one worker
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  Task *d_task = nullptr;
+  Task *h_task = nullptr;  // pinned staging
+  uint32_t *h_err = nullptr;  // pinned copy of the worker's error word
+  uint32_t *counter = nullptr;
+  bool ready = false;      // device state allocated
+  bool busy = false;
+  Request req{};
+};
+
+}  // namespace
+}  // namespace grus
+
+struct grus_server {
+  std::vector<grus_graph *> graphs;
+  grus::GraphDesc *d_graphs = nullptr;
+  uint64_t max_n = 0, max_m = 0;
+  int cluster = 8;
+  uint32_t huge = 8192, delta = 96;
+  uint64_t reserve = 1ull << 30;
+  std::vector<grus::Slot> slots;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<grus::Request> pending;
+  std::deque<grus_completion> completed;
+  std::thread worker;
+  std::atomic<bool> stop{false};
+  int device = 0;
+  uint64_t admitted = 0, finished = 0, rejected = 0;
+  int slots_ready = 0;
+  int error = GRUS_OK;
+};
+
+namespace grus {
+namespace {
+
+int slot_prepare(grus_server *s, Slot &sl) {
+  if (sl.ready) return GRUS_OK;
+  size_t free_b = 0, total_b = 0;
+  GRUS_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+  const size_t need = BatchState::bytes_per_worker(s->max_n, s->max_m, s->huge) + 4096;
+  if (free_b < need + s->reserve) return GRUS_ENOMEM;  // not admitted: wait for a slot
+  int rc = sl.state.reserve(1, s->max_n, s->max_m, s->huge);
+  if (rc) return rc;
+  GRUS_CUDA_TRY(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
+  GRUS_CUDA_TRY(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+  GRUS_CUDA_TRY(cudaMalloc(&sl.d_task, sizeof(Task)));
+  GRUS_CUDA_TRY(cudaMallocHost(&sl.h_task, sizeof(Task)));
+  GRUS_CUDA_TRY(cudaMallocHost(&sl.h_err, 4));
+  GRUS_CUDA_TRY(cudaMalloc(&sl.counter, 4));
+  GRUS_CUDA_TRY(cudaMemset(sl.state.err, 0, 4));
+  sl.ready = true;
+  ++s->slots_ready;
+  return GRUS_OK;
+}
+
+int slot_launch(grus_server *s, Slot &sl, const Request &r) {
+  Task &t = *sl.h_task;
+  t.graph = r.graph;
+  t.algo = r.algo;
+  t.src = r.src;
+  t.pad = 0;
+  t.out_off = 0;
+  GRUS_CUDA_TRY(cudaMemcpyAsync(sl.d_task, sl.h_task, sizeof(Task), cudaMemcpyHostToDevice, sl.stream));
+  GRUS_CUDA_TRY(cudaMemsetAsync(sl.counter, 0, 4, sl.stream));
+  int rc = batch_launch(sl.state, 0, 1, s->cluster, s->d_graphs, sl.d_task, 1, r.out, s->huge,
+                        s->delta, sl.counter, sl.stream);
+  if (rc) return rc;
+  GRUS_CUDA_TRY(cudaMemcpyAsync(sl.h_err, sl.state.err, 4, cudaMemcpyDeviceToHost, sl.stream));
+  GRUS_CUDA_TRY(cudaMemsetAsync(sl.state.err, 0, 4, sl.stream));
+  GRUS_CUDA_TRY(cudaEventRecord(sl.done, sl.stream));
+  return GRUS_OK;
+}
+
+void scheduler(grus_server *s) {
+  cudaSetDevice(s->device);
+  while (!s->stop.load()) {
+    bool idle = true;
+    // completions
+    for (auto &sl : s->slots) {
+      if (!sl.busy) continue;
+      const cudaError_t q = cudaEventQuery(sl.done);
+      if (q == cudaErrorNotReady) continue;
+      idle = false;
+      grus_completion c;
+      std::memset(&c, 0, sizeof(c));
+      c.tag = sl.req.tag;
+      c.status = q == cudaSuccess ? GRUS_OK : status_from_cuda(q);
+      if (q == cudaSuccess && *sl.h_err) c.status = status_from_device_error(*sl.h_err);
+      const auto now = Clock::now();
+      c.latency_us = std::chrono::duration<double, std::micro>(now - sl.req.t_submit).count();
+      sl.busy = false;
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->completed.push_back(c);
+      ++s->finished;
+      s->cv.notify_all();
+    }
+    // admissions
+    for (auto &sl : s->slots) {
+      if (sl.busy) continue;
+      Request r;
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->pending.empty()) break;
+        r = s->pending.front();
+      }
+      if (!sl.ready) {
+        const int rc = slot_prepare(s, sl);
+        if (rc == GRUS_ENOMEM && s->slots_ready > 0) continue;  // wait for a busy slot
+        if (rc == GRUS_ENOMEM) {
+          // not even one query fits in free HBM: refuse it rather than queue forever
+          grus_completion c;
+          std::memset(&c, 0, sizeof(c));
+          c.tag = r.tag;
+          c.status = GRUS_ENOMEM;
+          std::lock_guard<std::mutex> lk(s->mu);
+          s->pending.pop_front();
+          s->completed.push_back(c);
+          ++s->finished;
+          ++s->rejected;
+          s->cv.notify_all();
+          continue;
+        }
+        if (rc) {
+          std::lock_guard<std::mutex> lk(s->mu);
+          s->error = rc;
+          continue;
+        }
+      }
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->pending.pop_front();
+        ++s->admitted;
+      }
+      sl.req = r;
+      const int rc = slot_launch(s, sl, r);
+      if (rc) {
+        grus_completion c;
+        std::memset(&c, 0, sizeof(c));
+        c.tag = r.tag;
+        c.status = rc;
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->completed.push_back(c);
+        ++s->finished;
+        s->cv.notify_all();
+        continue;
+      }
+      sl.busy = true;
+      idle = false;
+    }
+    if (idle) {
+      std::unique_lock<std::mutex> lk(s->mu);
+      bool any_busy = false;
+      for (auto &sl : s->slots) any_busy |= sl.busy;
+      if (!any_busy && s->pending.empty())
+        s->cv.wait_for(lk, std::chrono::milliseconds(2));
+      else
+        std::this_thread::yield();
+    }
+  }
+}
+
+}  // namespace
+}  // namespace grus
+
+using namespace grus;
+
+extern "C" {
+
+int grus_server_create(grus_graph *const *graphs, int ngraphs, const grus_server_config *cfg,
+                       grus_server **out) {
+  if (!graphs || ngraphs < 1 || !out) return GRUS_EINVAL;
+  grus_server *s = new grus_server();
+  cudaGetDevice(&s->device);
+  std::vector<GraphDesc> descs;
+  for (int i = 0; i < ngraphs; ++i) {
+    if (!graphs[i]) {
+      delete s;
+      return GRUS_EINVAL;
+    }
+    s->graphs.push_back(graphs[i]);
+    descs.push_back(describe(graphs[i]));
+    s->max_n = std::max<uint64_t>(s->max_n, graphs[i]->n);
+    s->max_m = std::max<uint64_t>(s->max_m, graphs[i]->m);
+  }
+  int nslots = 16;
+  if (cfg) {
+    if (cfg->slots) nslots = (int)cfg->slots;
+    if (cfg->cluster_size) s->cluster = (int)cfg->cluster_size;
+    if (cfg->hbm_reserve_bytes) s->reserve = cfg->hbm_reserve_bytes;
+    if (cfg->sssp_delta) s->delta = cfg->sssp_delta;
+  }
+  if (s->cluster < 1 || s->cluster > 8 || nslots < 1 || nslots > 1024) {
+    delete s;
+    return GRUS_EINVAL;
+  }
+  s->slots.resize(nslots);
+  cudaError_t e = cudaMalloc(&s->d_graphs, ngraphs * sizeof(GraphDesc));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(s->d_graphs, descs.data(), ngraphs * sizeof(GraphDesc), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(s->d_graphs);
+    delete s;
+    set_last_error(cudaGetErrorString(e));
+    return status_from_cuda(e);
+  }
+  s->worker = std::thread(scheduler, s);
+  *out = s;
+  return GRUS_OK;
+}
+
+int grus_server_submit(grus_server *s, uint32_t graph, uint32_t algo, uint32_t src, uint32_t *out,
+                       uint64_t tag) {
+  if (!s || !out || graph >= s->graphs.size() || algo > GRUS_ALGO_SSSP) return GRUS_EINVAL;
+  const grus_graph *g = s->graphs[graph];
+  if (src >= g->n) return GRUS_EINVAL;
+  if (algo == GRUS_ALGO_SSSP && !g->csr.wts) return GRUS_EINVAL;
+  if (!is_device_pointer(out)) {
+    set_last_error("server outputs must be device (or managed) memory");
+    return GRUS_EINVAL;
+  }
+  Request r{tag, graph, algo, src, out, Clock::now()};
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->error) return s->error;
+    s->pending.push_back(r);
+  }
+  s->cv.notify_all();
+  return GRUS_OK;
+}
+
+int grus_server_poll(grus_server *s, grus_completion *out, int max, int wait_ms) {
+  if (!s || (!out && max > 0) || max < 0) return GRUS_EINVAL;
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (s->completed.empty() && wait_ms > 0)
+    s->cv.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return !s->completed.empty(); });
+  int k = 0;
+  while (k < max && !s->completed.empty()) {
+    out[k++] = s->completed.front();
+    s->completed.pop_front();
+  }
+  return k;
+}
+
+int grus_server_get_stats(grus_server *s, grus_server_stats *st) {
+  if (!s || !st) return GRUS_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  std::memset(st, 0, sizeof(*st));
+  st->submitted = s->admitted + s->pending.size();
+  st->admitted = s->admitted;
+  st->completed = s->finished;
+  st->pending = s->pending.size();
+  st->slots_ready = (uint32_t)s->slots_ready;
+  st->rejected = s->rejected;
+  st->slots = (uint32_t)s->slots.size();
+  return GRUS_OK;
+}
+
+int grus_server_destroy(grus_server *s) {
+  if (!s) return GRUS_EINVAL;
+  s->stop.store(true);
+  s->cv.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  for (auto &sl : s->slots) {
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    sl.state.release();
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+    if (sl.done) cudaEventDestroy(sl.done);
+    cudaFree(sl.d_task);
+    if (sl.h_task) cudaFreeHost(sl.h_task);
+    if (sl.h_err) cudaFreeHost(sl.h_err);
+    cudaFree(sl.counter);
+  }
+  cudaFree(s->d_graphs);
+  delete s;
+  return GRUS_OK;
+}
+
+}  // extern "C"

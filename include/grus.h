@@ -222,6 +222,83 @@ GRUS_API int grus_cc(grus_graph *g, uint32_t *label, grus_stats *stats, void *st
 GRUS_API int grus_pagerank(grus_graph *g, float damping, int iters, float *rank,
                   grus_stats *stats, void *stream);
 
+/* ---- batched queries ------------------------------------------------------ */
+/* Many BFS / SSSP queries over many resident graphs in one launch.  A worker
+ * is one thread-block cluster that takes queries from a device counter and
+ * runs each to completion (levels separated by the hardware cluster
+ * barrier); per-worker device state is sized for the largest graph.  The
+ * reference answers one query per process run. */
+#define GRUS_ALGO_BFS 0u
+#define GRUS_ALGO_SSSP 1u
+
+typedef struct grus_query {
+  uint32_t graph;        /* index into the graphs given at creation */
+  uint32_t algo;         /* GRUS_ALGO_BFS or GRUS_ALGO_SSSP */
+  uint32_t src;
+  uint32_t reserved;
+  uint64_t out_offset;   /* result = out + out_offset, n of the graph entries */
+} grus_query;
+
+typedef struct grus_batch_config {
+  uint32_t cluster_size; /* CTAs per worker (1..8, default 8) */
+  uint32_t workers;      /* 0 = as many as fit */
+  uint32_t huge_degree;  /* hub chunking threshold */
+  uint32_t sssp_delta;   /* SSSP bucket width */
+} grus_batch_config;
+
+typedef struct grus_batch grus_batch;
+
+GRUS_API int grus_batch_create(grus_graph *const *graphs, int ngraphs,
+                      const grus_batch_config *cfg, grus_batch **out);
+/* Runs queries[0..nq); `out` is device memory.  use_graph != 0 replays a
+ * captured CUDA graph (task upload, counter reset, kernel) re-captured only
+ * when nq, out or stream change.  Asynchronous unless stats is given. */
+GRUS_API int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *out,
+                   int use_graph, grus_stats *stats, void *stream);
+GRUS_API int grus_batch_get_info(const grus_batch *b, grus_batch_config *info);
+GRUS_API int grus_batch_free(grus_batch *b);
+
+/* ---- serving --------------------------------------------------------------- */
+/* A query server over device-resident graphs.  Requests queue on the host; a
+ * scheduler thread admits each into a worker slot (one cluster worker of the
+ * batch engine with its own device state and stream) as soon as a slot is
+ * free, allocating a slot's state only if free HBM covers it plus
+ * hbm_reserve_bytes.  Admitted queries overlap on the device.  Latency is
+ * measured from submit to observed completion on the host clock. */
+typedef struct grus_server grus_server;
+
+typedef struct grus_server_config {
+  uint32_t slots;            /* concurrent queries (default 16) */
+  uint32_t cluster_size;     /* CTAs per query (1..8, default 8) */
+  uint64_t hbm_reserve_bytes;/* free HBM kept back at admission (default 1 GiB) */
+  uint32_t sssp_delta;
+  uint32_t reserved;
+} grus_server_config;
+
+typedef struct grus_completion {
+  uint64_t tag;
+  int32_t status;
+  uint32_t reserved;
+  double latency_us;
+} grus_completion;
+
+typedef struct grus_server_stats {
+  uint64_t submitted, admitted, completed, pending, rejected;
+  uint32_t slots, slots_ready;
+} grus_server_stats;
+
+GRUS_API int grus_server_create(grus_graph *const *graphs, int ngraphs,
+                       const grus_server_config *cfg, grus_server **out);
+/* Queues one query; `out` (device memory, n of the graph entries) receives
+ * the depths (BFS) or distances (SSSP).  Returns at once. */
+GRUS_API int grus_server_submit(grus_server *s, uint32_t graph, uint32_t algo, uint32_t src,
+                       uint32_t *out, uint64_t tag);
+/* Collects up to max completions, waiting up to wait_ms for the first;
+ * returns how many were written. */
+GRUS_API int grus_server_poll(grus_server *s, grus_completion *out, int max, int wait_ms);
+GRUS_API int grus_server_get_stats(grus_server *s, grus_server_stats *st);
+GRUS_API int grus_server_destroy(grus_server *s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,96 @@
+"""GPU: batched queries (many graphs, many BFS/SSSP queries, one launch of
+cluster workers) -- every result bit-exact against the single-query path,
+plain launch and CUDA-graph replay, several cluster sizes."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def graphs(grus):
+    gs = []
+    for i, (scale, ef) in enumerate([(10, 8), (11, 16), (12, 32), (13, 8), (12, 16), (9, 4)]):
+        gs.append(grus.Graph.rmat(scale, ef, 100 + i, symmetric=True, weighted=True))
+    gs.append(grus.Graph.grid2d(40, 50, seed=7, weighted=True))
+    return gs
+
+
+def make_queries(grus, graphs, count, seed):
+    rng = np.random.default_rng(seed)
+    q = []
+    for _ in range(count):
+        gi = int(rng.integers(len(graphs)))
+        algo = int(rng.integers(2))
+        q.append((gi, algo, int(rng.integers(graphs[gi].n))))
+    return q
+
+
+def reference(grus, graphs, q):
+    gi, algo, src = q
+    return grus.sssp(graphs[gi], src) if algo == grus.ALGO_SSSP else grus.bfs(graphs[gi], src)
+
+
+@pytest.mark.parametrize("cluster", [1, 2, 8])
+def test_batch_matches_single_queries(grus, graphs, cluster):
+    torch = pytest.importorskip("torch")
+    b = grus.Batch(graphs, cluster_size=cluster)
+    queries = make_queries(grus, graphs, 96, cluster)
+    offs, total = b.layout(queries)
+    out = torch.full((total,), -7, dtype=torch.int32, device="cuda")
+    st = b.run(queries, out, offs, stats=True)
+    assert st["kernel_launches"] == 1
+    res = out.cpu().numpy().view(np.uint32)
+    for q, o in zip(queries, offs):
+        ref = reference(grus, graphs, q)
+        assert np.array_equal(res[o:o + len(ref)], ref), q
+    b.free()
+
+
+def test_batch_cuda_graph_replay(grus, graphs):
+    torch = pytest.importorskip("torch")
+    b = grus.Batch(graphs)
+    for rep in range(3):
+        queries = make_queries(grus, graphs, 64, 1000 + rep)
+        offs, total = b.layout(queries)
+        out = torch.zeros(total, dtype=torch.int32, device="cuda")
+        b.run(queries, out, offs, use_graph=True, stats=True)
+        res = out.cpu().numpy().view(np.uint32)
+        for q, o in zip(queries, offs):
+            ref = reference(grus, graphs, q)
+            assert np.array_equal(res[o:o + len(ref)], ref), (rep, q)
+    b.free()
+
+
+def test_batch_256_sssp_over_32_graphs(grus):
+    """The C4b shape at small scale: 256 SSSP queries over 32 resident graphs
+    of mixed scale and edge factor."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(4)
+    gs = [grus.Graph.rmat(int(rng.integers(8, 13)), int(rng.choice([8, 16, 32])), 500 + i,
+                          symmetric=True, weighted=True) for i in range(32)]
+    b = grus.Batch(gs)
+    queries = [(i % 32, grus.ALGO_SSSP, int(rng.integers(gs[i % 32].n))) for i in range(256)]
+    offs, total = b.layout(queries)
+    out = torch.zeros(total, dtype=torch.int32, device="cuda")
+    b.run(queries, out, offs, use_graph=True)
+    torch.cuda.synchronize()
+    res = out.cpu().numpy().view(np.uint32)
+    for q, o in zip(queries, offs):
+        ref = grus.sssp(gs[q[0]], q[2])
+        assert np.array_equal(res[o:o + len(ref)], ref)
+    b.free()
+
+
+def test_batch_rejects_bad_queries(grus, graphs):
+    torch = pytest.importorskip("torch")
+    b = grus.Batch(graphs)
+    out = torch.zeros(graphs[0].n, dtype=torch.int32, device="cuda")
+    with pytest.raises(grus.GrusError):
+        b.run([(0, grus.ALGO_BFS, graphs[0].n)], out, [0])
+    with pytest.raises(grus.GrusError):
+        b.run([(99, grus.ALGO_BFS, 0)], out, [0])
+    host = np.zeros(graphs[0].n, np.uint32)
+    with pytest.raises(grus.GrusError):
+        b.run([(0, grus.ALGO_BFS, 0)], host, [0])
+    b.free()

@@ -1,0 +1,67 @@
+"""GPU: the query server.  Every result must equal the same query run alone
+(bit-exact) while many queries overlap on the device; admission refuses work
+that does not fit in free HBM."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def graphs(grus):
+    return [grus.Graph.rmat(s, 16, 700 + s, symmetric=True, weighted=True) for s in (10, 12, 14, 15)]
+
+
+def drain(srv, want, timeout=120.0):
+    done = {}
+    t0 = time.time()
+    while len(done) < want and time.time() - t0 < timeout:
+        for tag, status, lat in srv.poll(256, wait_ms=50):
+            done[tag] = (status, lat)
+    return done
+
+
+def test_server_results_same_alone_and_in_mix(grus, graphs):
+    torch = pytest.importorskip("torch")
+    srv = grus.Server(graphs, slots=12, cluster_size=4)
+    rng = np.random.default_rng(5)
+    reqs, outs = [], []
+    for tag in range(120):
+        gi = int(rng.integers(len(graphs)))
+        algo = int(rng.integers(2))
+        src = int(rng.integers(graphs[gi].n))
+        out = torch.empty(graphs[gi].n, dtype=torch.int32, device="cuda")
+        reqs.append((gi, algo, src))
+        outs.append(out)
+        srv.submit(gi, algo, src, out, tag)
+    done = drain(srv, len(reqs))
+    assert len(done) == len(reqs)
+    assert all(st == 0 for st, _ in done.values())
+    for (gi, algo, src), out in zip(reqs, outs):
+        alone = grus.sssp(graphs[gi], src) if algo == grus.ALGO_SSSP else grus.bfs(graphs[gi], src)
+        assert np.array_equal(out.cpu().numpy().view(np.uint32), alone)
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["pending"] == 0 and st["slots_ready"] >= 1
+    srv.close()
+
+
+def test_server_admission_by_free_hbm(grus, graphs):
+    """A reserve larger than the device refuses every query with ENOMEM."""
+    torch = pytest.importorskip("torch")
+    srv = grus.Server(graphs, slots=4, hbm_reserve_bytes=1 << 50)
+    out = torch.empty(graphs[0].n, dtype=torch.int32, device="cuda")
+    srv.submit(0, grus.ALGO_BFS, 0, out, 1)
+    done = drain(srv, 1, timeout=30)
+    assert done[1][0] == grus.ENOMEM
+    assert srv.stats()["rejected"] == 1
+    srv.close()
+
+
+def test_server_rejects_bad_submissions(grus, graphs):
+    srv = grus.Server(graphs[:1], slots=2)
+    host = np.zeros(graphs[0].n, np.uint32)
+    with pytest.raises(grus.GrusError):
+        srv.submit(0, grus.ALGO_BFS, 0, host, 0)
+    srv.close()
