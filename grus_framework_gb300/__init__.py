@@ -144,6 +144,7 @@ def _load():
         "grus_server_poll": ([vp, C.POINTER(Completion), i32, i32], i32),
         "grus_server_get_stats": ([vp, C.POINTER(ServerStats)], i32),
         "grus_server_destroy": ([vp], i32),
+        "grus_autotune": ([vp, u32, u32, i32, C.POINTER(Tuning), C.POINTER(C.c_float)], i32),
         "grus_cc": ([vp, vp, C.POINTER(Stats), vp], i32),
         "grus_pagerank": ([vp, C.c_float, i32, vp, C.POINTER(Stats), vp], i32),
     }
@@ -508,3 +509,14 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def autotune(g: Graph, algo=ALGO_BFS, src=None, reps=2):
+    """Tunes the persistent kernel for `g` (stored on the graph); returns
+    (tuning dict, best device ms)."""
+    if src is None:
+        src = g.max_degree_vertex
+    t = Tuning()
+    ms = C.c_float()
+    _check(lib.grus_autotune(g._handle(), algo, src, reps, C.byref(t), C.byref(ms)), "grus_autotune")
+    return {k: getattr(t, k) for k, _ in t._fields_}, ms.value

@@ -38,6 +38,7 @@ SOURCES = [
     "msbfs.cu",
     "batch.cu",
     "serve.cu",
+    "tune.cu",
 ]
 
 

@@ -54,6 +54,10 @@ extern "C" {
 #define GRUS_GRAPH_SYMMETRIC 1u /* every edge (u,v) has (v,u): CSR == CSC */
 #define GRUS_GRAPH_WEIGHTED 2u  /* uint32 edge weights present */
 
+/* query kinds (batches, server, autotuner) */
+#define GRUS_ALGO_BFS 0u
+#define GRUS_ALGO_SSSP 1u
+
 /* generator flags */
 #define GRUS_GEN_SYMMETRIC 1u
 #define GRUS_GEN_WEIGHTED 2u
@@ -222,15 +226,21 @@ GRUS_API int grus_cc(grus_graph *g, uint32_t *label, grus_stats *stats, void *st
 GRUS_API int grus_pagerank(grus_graph *g, float damping, int iters, float *rank,
                   grus_stats *stats, void *stream);
 
+/* Autotuner: coordinate descent over the grus_tuning knobs of the BFS
+ * (alpha, beta, bu_words, huge_degree, ctas_per_sm) or SSSP (sssp_delta,
+ * huge_degree, ctas_per_sm) persistent kernel on this graph from `src`, each
+ * candidate timed best-of-`reps` with CUDA events.  Stores the fastest on the
+ * graph and returns it (and its time).  Outputs do not depend on the knobs.
+ * The reference has fixed launch shapes and thresholds. */
+GRUS_API int grus_autotune(grus_graph *g, uint32_t algo, uint32_t src, int reps,
+                  grus_tuning *best, float *best_ms);
+
 /* ---- batched queries ------------------------------------------------------ */
 /* Many BFS / SSSP queries over many resident graphs in one launch.  A worker
  * is one thread-block cluster that takes queries from a device counter and
  * runs each to completion (levels separated by the hardware cluster
  * barrier); per-worker device state is sized for the largest graph.  The
  * reference answers one query per process run. */
-#define GRUS_ALGO_BFS 0u
-#define GRUS_ALGO_SSSP 1u
-
 typedef struct grus_query {
   uint32_t graph;        /* index into the graphs given at creation */
   uint32_t algo;         /* GRUS_ALGO_BFS or GRUS_ALGO_SSSP */
