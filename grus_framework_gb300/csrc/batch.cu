@@ -317,7 +317,22 @@ __global__ void __launch_bounds__(kBatchBlock) batch_kernel(Args a) {
 // ---------------------------------------------------------------------------
 using namespace batch;
 
+// Clusters of up to 16 CTAs: sizes above the portable 8 need an opt-in per
+// kernel (set once per process).
+static int allow_wide_clusters() {
+  static int done = 0;
+  if (!done) {
+    GRUS_CUDA_TRY(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    done = 1;
+  }
+  return GRUS_OK;
+}
+
 int batch_occupancy(int cluster, int *workers) {
+  if (cluster > 8) {
+    const int rc = allow_wide_clusters();
+    if (rc) return rc;
+  }
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cudaLaunchAttribute attr;
@@ -439,7 +454,7 @@ struct grus_batch {
   grus::Task *d_tasks = nullptr, *h_tasks = nullptr;  // pinned staging
   uint32_t task_cap = 0;
   grus::BatchState state;
-  int cluster = 8, workers = 0;
+  int cluster = 16, workers = 0;
   uint32_t huge = 8192, delta = 96;
   uint64_t max_n = 0, max_m = 0, total_out = 0;
   cudaGraph_t graph = nullptr;
@@ -477,9 +492,9 @@ int grus_batch_create(grus_graph *const *graphs, int ngraphs, const grus_batch_c
     if (cfg->sssp_delta) b->delta = cfg->sssp_delta;
     if (cfg->workers) b->workers = (int)cfg->workers;
   }
-  if (b->cluster < 1 || b->cluster > 8) {
+  if (b->cluster < 1 || b->cluster > 16) {
     delete b;
-    set_last_error("cluster_size must be 1..8");
+    set_last_error("cluster_size must be 1..16");
     return GRUS_EINVAL;
   }
   int maxw = 0;

@@ -231,11 +231,17 @@ int grus_server_create(grus_graph *const *graphs, int ngraphs, const grus_server
     if (cfg->hbm_reserve_bytes) s->reserve = cfg->hbm_reserve_bytes;
     if (cfg->sssp_delta) s->delta = cfg->sssp_delta;
   }
-  if (s->cluster < 1 || s->cluster > 8 || nslots < 1 || nslots > 1024) {
+  if (s->cluster < 1 || s->cluster > 16 || nslots < 1 || nslots > 1024) {
     delete s;
     return GRUS_EINVAL;
   }
   s->slots.resize(nslots);
+  int probe_workers = 0;
+  if (batch_occupancy(s->cluster, &probe_workers) != GRUS_OK || probe_workers < 1) {
+    delete s;
+    set_last_error("server: no cluster of this size can be resident");
+    return GRUS_EINVAL;
+  }
   cudaError_t e = cudaMalloc(&s->d_graphs, ngraphs * sizeof(GraphDesc));
   if (e == cudaSuccess)
     e = cudaMemcpy(s->d_graphs, descs.data(), ngraphs * sizeof(GraphDesc), cudaMemcpyHostToDevice);

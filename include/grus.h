@@ -250,7 +250,7 @@ typedef struct grus_query {
 } grus_query;
 
 typedef struct grus_batch_config {
-  uint32_t cluster_size; /* CTAs per worker (1..8, default 8) */
+  uint32_t cluster_size; /* CTAs per worker (1..16, default 16) */
   uint32_t workers;      /* 0 = as many as fit */
   uint32_t huge_degree;  /* hub chunking threshold */
   uint32_t sssp_delta;   /* SSSP bucket width */
@@ -279,7 +279,7 @@ typedef struct grus_server grus_server;
 
 typedef struct grus_server_config {
   uint32_t slots;            /* concurrent queries (default 16) */
-  uint32_t cluster_size;     /* CTAs per query (1..8, default 8) */
+  uint32_t cluster_size;     /* CTAs per query (1..16, default 8) */
   uint64_t hbm_reserve_bytes;/* free HBM kept back at admission (default 1 GiB) */
   uint32_t sssp_delta;
   uint32_t reserved;
