@@ -378,6 +378,7 @@ int BatchState::reserve(int nworkers, uint64_t max_n, uint64_t max_m, uint32_t h
   if (e == cudaSuccess) e = cudaMalloc(&ctl, (uint64_t)nworkers * sizeof(WorkerCtl));
   if (e == cudaSuccess) e = cudaMalloc(&counter, 4);
   if (e == cudaSuccess) e = cudaMalloc(&err, 4);
+  if (e == cudaSuccess) e = cudaMemset(err, 0, 4);  // read back after every run
   if (e != cudaSuccess) {
     cudaGetLastError();
     release();

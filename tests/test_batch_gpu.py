@@ -94,3 +94,16 @@ def test_batch_rejects_bad_queries(grus, graphs):
     with pytest.raises(grus.GrusError):
         b.run([(0, grus.ALGO_BFS, 0)], host, [0])
     b.free()
+
+
+def test_batch_single_worker_high_diameter(grus, oracle_mod):
+    """One cluster worker on a long path-like grid: many levels, each ended by
+    the hardware cluster barrier; fresh state reports no error."""
+    torch = pytest.importorskip("torch")
+    g = grus.Graph.grid2d(300, 40)
+    for cl in (16, 4):
+        b = grus.Batch([g], cluster_size=cl, workers=1)
+        out = torch.zeros(g.n, dtype=torch.int32, device="cuda")
+        b.run([(0, grus.ALGO_BFS, 41)], out, [0], stats=True)
+        assert np.array_equal(out.cpu().numpy().view(np.uint32), grus.bfs(g, 41))
+        b.free()
