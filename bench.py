@@ -1,25 +1,32 @@
 #!/usr/bin/env python3
-"""Headline benchmark: single-query BFS throughput on RMAT scale 24.
+"""Traversal benchmark: single-query BFS throughput on RMAT scale 24 (default).
 
-Workload (the spec traversal target): RMAT scale 24, edge factor 16,
-a/b/c/d = .57/.19/.19/.05, seed 3, symmetrised, self-loops and duplicates
-removed, seeded vertex relabelling; source = first vertex of maximum
-out-degree (the rule of include/graph_loader.cuh:132-137).  Synthetic data:
-the reference's datasets are not available; the graph is generated on the
-device from the seed.
+Default workload (the traversal-rate target of the path): RMAT scale 24,
+edge factor 16, a/b/c/d = .57/.19/.19/.05, seed 3, symmetrised, self-loops
+and duplicates removed, seeded vertex relabelling; source = first vertex of
+maximum out-degree (the rule of include/graph_loader.cuh:132-137).  Synthetic
+data: the reference's datasets are not available; graphs are generated on
+the device from the seed.
 
-A step is one BFS from the source over the resident graph.  Metric: GTEPS =
-m_r / time, m_r = sum of out-degrees of reached vertices.  `value` is timed
-with CUDA events on the launching stream (device-resident input and output);
-`e2e` is the same BFS through the public API with a pinned HOST output buffer
-(the depth array is copied back inside the timed region).  L2 is flushed
-(256 MB write) before every timed step, outside its events.
+A step is one query over the resident graph.  Metric: GTEPS = traversed
+edges / time (BFS/SSSP: m_r = sum of out-degrees of reached vertices; CC: m;
+PageRank: m x iterations; 64-source BFS: the sum of m_r over the sources).
+`value` is timed with CUDA events on the launching stream (device-resident
+input and output); `e2e` is the same query through the public API with a
+pinned HOST output buffer (the result is copied back inside the timed
+region).  L2 is flushed (256 MB write) before every timed step, outside its
+events.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl grus|reference]
+                  [--workload NAME] [--scale S]
 
-`--impl reference` times the CPU path (the reference has no host BFS; the
-plain OpenMP level-synchronous BFS of the oracle stands in) on all host cores
-on the same graph, generated on the host from the same seed.
+Other workloads (`--workload`): sssp-rmat22, cc-rmat22, pagerank-rmat24
+(directed), bfs-grid4096, msbfs-rmat23 (64 sources).  `--scale` overrides
+the RMAT scale (or the grid side as a power of two) for small profiling runs.
+
+`--impl reference` times the CPU path (the reference has no host traversal;
+the plain OpenMP version of the same algorithm in the oracle stands in) on
+all host cores on the same graph, generated on the host from the same seed.
 Under torchrun each rank runs an independent replica ("replicas only").
 """
 from __future__ import annotations
@@ -39,11 +46,30 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-WORKLOAD = dict(workload="bfs_rmat24_sym", graph="rmat", scale=24, edge_factor=16, seed=3,
-                symmetric=True, relabel=True, source="max_degree_vertex")
-METRIC = "GTEPS (single-query BFS, RMAT-24 symmetrised)"
-UNIT = "GTEPS"
 FALLBACK_HBM_GBS = 6800.0
+UNIT = "GTEPS"
+INFINIT = 4294967294
+
+WORKLOADS = {
+    "bfs-rmat24": dict(algo="bfs", graph="rmat", scale=24, edge_factor=16, seed=3,
+                       symmetric=True, weighted=False, kernel="bfs_persistent",
+                       metric="GTEPS (single-query BFS, RMAT-24 symmetrised)"),
+    "sssp-rmat22": dict(algo="sssp", graph="rmat", scale=22, edge_factor=16, seed=2,
+                        symmetric=True, weighted=True, kernel="sssp_persistent",
+                        metric="GTEPS (single-query SSSP, RMAT-22 symmetrised, w in [1,255])"),
+    "cc-rmat22": dict(algo="cc", graph="rmat", scale=22, edge_factor=16, seed=2,
+                      symmetric=True, weighted=False, kernel="cc (all kernels)",
+                      metric="GTEPS (connected components, RMAT-22 symmetrised)"),
+    "pagerank-rmat24": dict(algo="pagerank", graph="rmat", scale=24, edge_factor=16, seed=3,
+                            symmetric=False, weighted=False, kernel="pr_persistent", iters=20,
+                            metric="GTEPS (pull PageRank, 20 iterations, RMAT-24 directed)"),
+    "bfs-grid4096": dict(algo="bfs", graph="grid", scale=12, seed=0, kernel="bfs_persistent",
+                         metric="GTEPS (single-query BFS, 4096x4096 grid, source 4097)"),
+    "msbfs-rmat23": dict(algo="msbfs", graph="rmat", scale=23, edge_factor=16, seed=4,
+                         symmetric=True, weighted=False, kernel="msbfs_persistent", sources=64,
+                         metric="GTEPS (64-source BFS in one launch, RMAT-23 symmetrised)"),
+}
+DEFAULT_WORKLOAD = "bfs-rmat24"
 
 
 def measured_peaks():
@@ -54,11 +80,28 @@ def measured_peaks():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def bfs_alg_bytes(n, nr, mr):
-    """Algorithmic bytes of one BFS: 4(n+1) offsets + 4 m_r column ids + 4n depth
-    writes + 8 n_r frontier enqueue/dequeue (the fixed top-down figure, also
-    used for direction-optimised runs)."""
-    return 4 * (n + 1) + 4 * mr + 4 * n + 8 * nr
+def alg_bytes(algo, n, m, nr, mr, iters=1, sources=1):
+    """Algorithmic bytes of one launch.
+
+    bfs:  4(n+1) offsets + 4 m_r column ids + 4n depth writes + 8 n_r frontier
+          enqueue/dequeue (the top-down figure, also used for direction-
+          optimised runs);
+    sssp: as bfs with 8 m_r (column id + weight per relaxed edge);
+    cc:   4(n+1) + 4m + 8n (labels read and written once);
+    pagerank: per iteration 4(n+1) + 8m (column id + contribution) + 8n;
+    msbfs: 4(n+1) + 4m + 8n (visit/frontier words) + 4 * sources * n depths.
+    """
+    if algo == "bfs":
+        return 4 * (n + 1) + 4 * mr + 4 * n + 8 * nr
+    if algo == "sssp":
+        return 4 * (n + 1) + 8 * mr + 4 * n + 8 * nr
+    if algo == "cc":
+        return 4 * (n + 1) + 4 * m + 8 * n
+    if algo == "pagerank":
+        return iters * (4 * (n + 1) + 8 * m + 8 * n)
+    if algo == "msbfs":
+        return 4 * (n + 1) + 4 * m + 8 * n + 4 * sources * n
+    raise ValueError(algo)
 
 
 class ClockSampler:
@@ -81,6 +124,7 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            time.sleep(0.3)  # first sample before the timed region
         except Exception:
             self.proc = None
         return self
@@ -135,22 +179,21 @@ def init_dist(ws):
     return dist
 
 
-def reduce_max(dist, x):
+def reduce_op(dist, x, op):
     if dist is None:
         return x
     import torch
     t = torch.tensor([float(x)], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=op(dist))
     return float(t.item())
+
+
+def reduce_max(dist, x):
+    return reduce_op(dist, x, lambda d: d.ReduceOp.MAX)
 
 
 def reduce_sum(dist, x):
-    if dist is None:
-        return x
-    import torch
-    t = torch.tensor([float(x)], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return reduce_op(dist, x, lambda d: d.ReduceOp.SUM)
 
 
 def barrier(dist):
@@ -158,44 +201,140 @@ def barrier(dist):
         dist.barrier()
 
 
+def workload_spec(args):
+    w = dict(WORKLOADS[args.workload])
+    if args.scale:
+        w["scale"] = args.scale
+    w["workload"] = args.workload if not args.scale else f"{args.workload}@scale{args.scale}"
+    return w
+
+
+def grid_source(side):
+    return side + 1  # vertex (1, 1)
+
+
+def msbfs_sources(n, offs_or_degree_fn, k, seed):
+    """k distinct sources with degree > 0 drawn with a seeded generator."""
+    rng = np.random.default_rng(seed)
+    out = []
+    seen = set()
+    while len(out) < k:
+        v = int(rng.integers(n))
+        if v not in seen and offs_or_degree_fn(v) > 0:
+            seen.add(v)
+            out.append(v)
+    return np.array(out, dtype=np.uint32)
+
+
 # ---------------------------------------------------------------------------
-def cpu_baseline_bfs(offs, cols, src, budget_s=12.0, max_runs=5):
-    """OpenMP top-down BFS of the oracle on all host threads; median GTEPS."""
+# CPU path (the oracle's OpenMP versions; bounded samples)
+def cpu_run(w, csr, csc, src, srcs, threads, budget_s=12.0, max_runs=5):
+    """Times the OpenMP version of the workload's algorithm on `threads` host
+    threads.  Returns (units per second, sample description)."""
     import oracle
-    g = oracle.CSR(offs, cols)
-    threads = oracle.omp_threads()
-    d, _ = oracle.omp_bfs(g, src, threads)  # warm-up
-    mr = oracle.reached_edges(g, d)
-    times = []
+    algo = w["algo"]
+    times, units = [], 0
     t_start = time.perf_counter()
-    while len(times) < max_runs and (time.perf_counter() - t_start) < budget_s:
-        _, t = oracle.omp_bfs(g, src, threads)
-        times.append(t)
+    if algo in ("bfs", "sssp"):
+        fn = oracle.omp_bfs if algo == "bfs" else oracle.omp_sssp
+        d, _ = fn(csr, src, threads)
+        units = oracle.reached_edges(csr, d)
+        while len(times) < max_runs and (not times or time.perf_counter() - t_start < budget_s):
+            times.append(fn(csr, src, threads)[1])
+        desc = f"{len(times)} full {algo.upper()} runs from the source"
+    elif algo == "cc":
+        oracle.omp_cc(csr, threads)
+        units = csr.m
+        while len(times) < max_runs and (not times or time.perf_counter() - t_start < budget_s):
+            times.append(oracle.omp_cc(csr, threads)[1])
+        desc = f"{len(times)} full CC runs"
+    elif algo == "pagerank":
+        outdeg = np.diff(csr.offs.astype(np.int64)).astype(np.uint32)
+        it = 2  # bounded sample: 2 iterations, rate per iteration-edge
+        oracle.omp_pagerank(csc, outdeg, 0.85, it, threads)
+        units = csr.m * it
+        while len(times) < max_runs and (not times or time.perf_counter() - t_start < budget_s):
+            times.append(oracle.omp_pagerank(csc, outdeg, 0.85, it, threads)[1])
+        desc = f"{len(times)} runs of {it} pull iterations"
+    elif algo == "msbfs":
+        per = []
+        for s in srcs[:4]:  # bounded sample: 4 of the 64 sources, one BFS each
+            d, t = oracle.omp_bfs(csr, int(s), threads)
+            per.append((oracle.reached_edges(csr, d), t))
+        units = sum(p[0] for p in per)
+        times = [sum(p[1] for p in per)]
+        desc = "one OpenMP BFS from each of the first 4 of the 64 sources"
     med = statistics.median(times)
-    return {"value": round(mr / med / 1e9, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{len(times)} full BFS runs from the same source on the same graph "
-                      f"(median {med*1e3:.1f} ms), OpenMP level-synchronous top-down BFS"}
+    return units / med / 1e9, f"{desc}, median {med*1e3:.1f} ms, OpenMP level-synchronous"
 
 
+def host_graph(w):
+    """The workload's graph generated on the host by the oracle (same bits)."""
+    import oracle
+    if w["graph"] == "grid":
+        side = 1 << w["scale"]
+        return oracle.grid(side, side, w.get("seed", 0), 0)
+    flags = ((oracle.GEN_SYMMETRIC if w["symmetric"] else 0)
+             | (oracle.GEN_WEIGHTED if w["weighted"] else 0) | oracle.GEN_RELABEL)
+    return oracle.rmat(w["scale"], w["edge_factor"], w["seed"], flags)
+
+
+# ---------------------------------------------------------------------------
 def run_grus(args, dist, rank, local):
     import torch
     import grus_framework_gb300 as grus
 
     torch.cuda.set_device(local)
     grus.device_init(local)
-    w = WORKLOAD
-    g = grus.Graph.rmat(w["scale"], w["edge_factor"], w["seed"], symmetric=w["symmetric"],
-                        relabel=w["relabel"])
-    n, m, src = g.n, g.m, g.max_degree_vertex
+    w = workload_spec(args)
+    algo = w["algo"]
+    if w["graph"] == "grid":
+        side = 1 << w["scale"]
+        g = grus.Graph.grid2d(side, side, w.get("seed", 0))
+        src = grid_source(side)
+    else:
+        g = grus.Graph.rmat(w["scale"], w["edge_factor"], w["seed"], symmetric=w["symmetric"],
+                            weighted=w["weighted"], relabel=True)
+        src = g.max_degree_vertex
+    n, m = g.n, g.m
     stream = torch.cuda.Stream()
-    out_dev = torch.empty(n, dtype=torch.int32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    srcs = None
+    iters = w.get("iters", 1)
+    k = w.get("sources", 1)
+    if algo == "msbfs":
+        offs_h = None
+        offs_h, _, _ = g.copy_csr()
+        srcs = msbfs_sources(n, lambda v: int(offs_h[v + 1]) - int(offs_h[v]), k, 4)
+        del offs_h
+    if algo == "pagerank":
+        g.build_csc()
 
-    # one call with stats: m_r, n_r (deterministic for the source), kernel time
-    _, st = grus.bfs(g, src, out=out_dev, stream=stream, stats=True)
-    mr, nr = st["edges_reached"], st["vertices_reached"]
+    def make_out(host):
+        shape = (k, n) if algo == "msbfs" else (n,)
+        dt = torch.float32 if algo == "pagerank" else torch.int32
+        if host:
+            return torch.empty(shape, dtype=dt, pin_memory=True)
+        return torch.empty(shape, dtype=dt, device="cuda")
+
+    def call(out, stats=False):
+        if algo == "bfs":
+            return grus.bfs(g, src, out=out, stream=stream, stats=stats)
+        if algo == "sssp":
+            return grus.sssp(g, src, out=out, stream=stream, stats=stats)
+        if algo == "cc":
+            return grus.cc(g, out=out, stream=stream, stats=stats)
+        if algo == "pagerank":
+            return grus.pagerank(g, 0.85, iters, out=out, stream=stream, stats=stats)
+        return grus.bfs_multi(g, srcs, out=out, stream=stream, stats=stats)
+
+    out_dev = make_out(False)
+    _, st = call(out_dev, stats=True)
+    nr, mr = st["vertices_reached"], st["edges_reached"]
+    launches = max(int(st["kernel_launches"]), 1)
+    units = {"bfs": mr, "sssp": mr, "cc": m, "pagerank": m * iters, "msbfs": mr}[algo]
     for _ in range(args.warmup):
-        grus.bfs(g, src, out=out_dev, stream=stream)
+        call(out_dev)
     torch.cuda.synchronize()
     barrier(dist)
 
@@ -206,66 +345,93 @@ def run_grus(args, dist, rank, local):
             with torch.cuda.stream(stream):
                 flush.zero_()
             ev[i][0].record(stream)
-            grus.bfs(g, src, out=out_dev, stream=stream)
+            call(out_dev)
             ev[i][1].record(stream)
         torch.cuda.synchronize()
     barrier(dist)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = reduce_max(dist, sum(step_ms))
     ws = dist.get_world_size() if dist else 1
-    total_edges = reduce_sum(dist, mr * args.steps)
-    value = total_edges / (total_ms * 1e-3) / 1e9
+    total_units = reduce_sum(dist, units * args.steps)
+    value = total_units / (total_ms * 1e-3) / 1e9
     mean_ms = sum(step_ms) / len(step_ms)
 
     # end to end through the public API: pinned host output, D2H inside
-    out_host = torch.empty(n, dtype=torch.int32, pin_memory=True)
-    grus.bfs(g, src, out=out_host, stream=stream)
+    out_host = make_out(True)
+    call(out_host)
     e2e_s = []
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
         stream.synchronize()
         t0 = time.perf_counter()
-        grus.bfs(g, src, out=out_host, stream=stream)
+        call(out_host)
         e2e_s.append(time.perf_counter() - t0)
     e2e_total = reduce_max(dist, sum(e2e_s))
-    e2e_value = total_edges / e2e_total / 1e9
+    e2e_value = total_units / e2e_total / 1e9
+    d2h = out_host.numel() * 4
+    h2d = 4 * (k if algo == "msbfs" else (1 if algo in ("bfs", "sssp") else 0))
 
-    # correctness of the timed configuration (cheap checks; full parity in tests)
-    d = out_host.numpy().view(np.uint32)
-    assert d[src] == 0 and int(np.count_nonzero(d != 4294967294)) == nr
+    # cheap checks of the timed configuration (full parity lives in tests/)
+    res = out_host.numpy()
+    if algo in ("bfs", "sssp"):
+        d = res.view(np.uint32)
+        assert d[src] == 0 and int(np.count_nonzero(d != INFINIT)) == nr
+    elif algo == "msbfs":
+        d = res.view(np.uint32)
+        assert all(d[i, s] == 0 for i, s in enumerate(srcs))
+    elif algo == "cc":
+        lab = res.view(np.uint32)
+        assert np.all(lab <= np.arange(n, dtype=np.uint32))
+    else:
+        assert np.isfinite(res).all()
 
     peak, peak_kind = measured_peaks()
-    alg = bfs_alg_bytes(n, nr, mr)
+    alg = alg_bytes(algo, n, m, nr, mr, iters, k)
     achieved = alg / (mean_ms * 1e-3) / 1e9
-    traffic = None
-    prof = ROOT / "profiles" / "bfs_persistent_rmat24.json"
+    traffic, traffic_note = None, None
+    prof = ROOT / "profiles" / "dram_traffic.json"
     if prof.exists():
-        traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
+        rec = json.loads(prof.read_text()).get(w["workload"])
+        if rec:
+            traffic, traffic_note = rec.get("dram_bytes_per_launch"), rec.get("note")
     result = None
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            offs, cols, _ = g.copy_csr()
-            cpu = cpu_baseline_bfs(offs, cols, src)
+            import oracle
+            offs, cols, wts = g.copy_csr()
+            csr = oracle.CSR(offs, cols, wts)
+            csc = None
+            if algo == "pagerank":
+                co, cc_, _ = g.copy_csc()
+                csc = oracle.CSR(co, cc_)
+            threads = oracle.omp_threads()
+            v, sample = cpu_run(w, csr, csc, src, srcs, threads)
+            cpu = {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": sample}
         clocks = clk.summary()
+        cfg = {k_: v_ for k_, v_ in w.items() if k_ not in ("metric", "kernel")}
+        cfg.update({"n": n, "m": m, "src": src if algo != "msbfs" else "64 seeded (seed 4)",
+                    "l2": "flushed (256 MB write) before each step",
+                    "parallelism": f"replicas x{ws}", "levels": st["levels"],
+                    "bottom_up_levels": st["bottom_up_levels"],
+                    "vertices_reached": nr, "edges_reached": mr})
         result = {
-            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
+            "metric": w["metric"], "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(mean_ms, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic (RMAT generated on device from the seed)",
-            "config": {**w, "n": n, "m": m, "src": src, "l2": "flushed (256 MB write) before each step",
-                       "parallelism": f"replicas x{ws}", "levels": st["levels"],
-                       "bottom_up_levels": st["bottom_up_levels"],
-                       "vertices_reached": nr, "edges_reached": mr},
-            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 4,
-                    "d2h_bytes_per_step": 4 * n,
-                    "note": "grus_bfs with a pinned host output buffer; graph resident in HBM"},
-            "gpu_launches": args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if algo == "pagerank" else "u32",
+            "data": "synthetic (generated on device from the seed)",
+            "config": cfg,
+            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "note": "public API call with a pinned host output buffer; graph resident in HBM"},
+            "gpu_launches": launches * args.steps,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "peak_source": peak_kind, "kernel": "bfs_persistent",
-                         "algorithmic_bytes_per_launch": alg},
+                         "traffic_note": traffic_note, "peak_source": peak_kind,
+                         "kernel": w["kernel"], "algorithmic_bytes_per_launch": alg},
             "cpu_baseline": cpu,
             "clocks": clocks,
         }
@@ -274,30 +440,37 @@ def run_grus(args, dist, rank, local):
 
 
 def run_reference(args, dist, rank):
-    """CPU path: OpenMP BFS of the oracle on the host cores (rank 0 only)."""
+    """CPU path: the oracle's OpenMP version on the host cores (rank 0 only)."""
     if rank != 0:
         return None
     import oracle
-    w = WORKLOAD
-    flags = oracle.GEN_SYMMETRIC | (oracle.GEN_RELABEL if w["relabel"] else 0)
-    g = oracle.rmat(w["scale"], w["edge_factor"], w["seed"], flags)
-    src = oracle.max_degree_vertex(g)
+    w = workload_spec(args)
+    algo = w["algo"]
+    g = host_graph(w)
+    src = grid_source(1 << w["scale"]) if w["graph"] == "grid" else oracle.max_degree_vertex(g)
+    csc = oracle.csr_to_csc(g) if algo == "pagerank" else None
+    srcs = None
+    if algo == "msbfs":
+        srcs = msbfs_sources(g.n, lambda v: int(g.offs[v + 1]) - int(g.offs[v]), 64, 4)
     threads = oracle.omp_threads()
-    d, _ = oracle.omp_bfs(g, src, threads)
-    mr = oracle.reached_edges(g, d)
     for _ in range(max(args.warmup - 1, 0)):
-        oracle.omp_bfs(g, src, threads)
-    times = [oracle.omp_bfs(g, src, threads)[1] for _ in range(args.steps)]
-    total = sum(times)
-    value = mr * args.steps / total / 1e9
+        cpu_run(w, g, csc, src, srcs, threads, budget_s=0.0, max_runs=1)
+    rates = []
+    sample = ""
+    for _ in range(args.steps):
+        r, sample = cpu_run(w, g, csc, src, srcs, threads, budget_s=0.0, max_runs=1)
+        rates.append(r)
+    value = statistics.median(rates)
+    cfg = {k_: v_ for k_, v_ in w.items() if k_ not in ("metric", "kernel")}
+    cfg.update({"n": g.n, "m": g.m, "src": src})
     return {
-        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total / args.steps * 1e3, 2),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-        "data": "synthetic (RMAT generated on the host from the seed)", "impl": "reference",
-        "config": {**w, "n": g.n, "m": g.m, "src": src, "edges_reached": mr},
+        "metric": w["metric"], "value": round(value, 4), "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if algo == "pagerank" else "u32",
+        "data": "synthetic (generated on the host from the seed)", "impl": "reference",
+        "config": cfg,
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "each step = one full OpenMP BFS from the source"},
+                         "sample": f"each step: {sample}"},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -308,9 +481,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["grus", "reference"], default="grus")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--scale", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "grus" else args.warmup
+    if args.impl == "grus":
+        args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
     dist = init_dist(ws)
     if args.impl == "reference":
