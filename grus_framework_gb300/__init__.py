@@ -84,7 +84,7 @@ class BatchConfig(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_uint32), ("cluster_size", C.c_uint32),
                 ("hbm_reserve_bytes", C.c_uint64), ("sssp_delta", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("big_edges", C.c_uint32)]
 
 
 class Completion(C.Structure):
@@ -95,7 +95,8 @@ class Completion(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
                 ("pending", C.c_uint64), ("rejected", C.c_uint64), ("slots", C.c_uint32),
-                ("slots_ready", C.c_uint32)]
+                ("slots_ready", C.c_uint32), ("big_launches", C.c_uint64),
+                ("big_queries", C.c_uint64)]
 
 
 class Tuning(C.Structure):
@@ -134,6 +135,7 @@ def _load():
         "grus_bfs": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
         "grus_sssp": ([vp, u32, vp, C.POINTER(Stats), vp], i32),
         "grus_bfs_trace": ([vp, C.POINTER(LevelTrace), i32], i32),
+        "grus_sssp_trace": ([vp, C.POINTER(LevelTrace), i32], i32),
         "grus_bfs_multi": ([vp, vp, i32, vp, C.POINTER(Stats), vp], i32),
         "grus_batch_create": ([C.POINTER(vp), i32, C.POINTER(BatchConfig), PG], i32),
         "grus_batch_run": ([vp, C.POINTER(Query), i32, vp, i32, C.POINTER(Stats), vp], i32),
@@ -387,6 +389,17 @@ def bfs_trace(g: Graph, max_levels: int = 128):
                  pull=bool(buf[i].pull)) for i in range(k)]
 
 
+def sssp_trace(g: Graph, max_levels: int = 256):
+    """Per-level records of the last sssp(..., stats=True) call on `g`:
+    relaxations, frontier entries and threshold advances so far."""
+    buf = (LevelTrace * max_levels)()
+    k = lib.grus_sssp_trace(g._handle(), buf, max_levels)
+    if k < 0:
+        _check(k, "grus_sssp_trace")
+    return [dict(end_us=buf[i].end_ns / 1e3, relaxations=buf[i].edges,
+                 frontier=buf[i].vertices, splits=buf[i].pull) for i in range(k)]
+
+
 def sssp(g: Graph, src: int, out=None, stream=None, stats: bool = False):
     """Exact shortest-path distances from `src` over the uint32 edge weights."""
     out = _out_array(g, out, np.uint32)
@@ -475,9 +488,10 @@ class Batch:
 class Server:
     """Query server over resident graphs (include/grus.h grus_server_*)."""
 
-    def __init__(self, graphs, slots=16, cluster_size=8, hbm_reserve_bytes=0, sssp_delta=0):
+    def __init__(self, graphs, slots=16, cluster_size=8, hbm_reserve_bytes=0, sssp_delta=0,
+                 big_edges=0):
         self.graphs = list(graphs)
-        cfg = ServerConfig(slots, cluster_size, hbm_reserve_bytes, sssp_delta, 0)
+        cfg = ServerConfig(slots, cluster_size, hbm_reserve_bytes, sssp_delta, big_edges)
         h = C.c_void_p()
         _check(lib.grus_server_create(_graph_array(self.graphs), len(self.graphs), C.byref(cfg),
                                       C.byref(h)), "grus_server_create")

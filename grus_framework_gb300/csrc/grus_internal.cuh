@@ -78,4 +78,10 @@ bool is_device_pointer(const void *p);
 int launch_persistent(const void *fn, void **args, int block, int per_sm_req,
                       int occupancy, cudaStream_t s, void *win_base, size_t win_bytes);
 
+// Multi-source BFS (msbfs.cu): outs[i] (device memory, n entries) receives
+// the depths from hsrc[i] (host array), 1 <= k <= 64.  With stats the call
+// waits for the launch and checks its error word.
+int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
+              grus_stats *stats, cudaStream_t s);
+
 }  // namespace grus

@@ -28,6 +28,7 @@ namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
+constexpr uint32_t kPullLane = 32;  // in-edges a lane scans alone in a pull level
 constexpr uint32_t kDefHuge = 8192;
 constexpr float kDefAlpha = 15.f;
 
@@ -54,7 +55,7 @@ struct Args {
   uint64_t m;
   int k;
   const uint32_t *srcs;
-  uint32_t *depth;
+  uint32_t *out[64];  // depth array of each source (n entries each)
   unsigned long long full;
   unsigned long long *visit, *front[2];
   uint32_t *touched[2];
@@ -83,7 +84,7 @@ __device__ __forceinline__ void write_depths(const Args &a, uint32_t u, unsigned
   while (wor) {
     const int kb = __ffsll((long long)wor) - 1;
     wor &= wor - 1;
-    if ((bits >> kb) & 1ull) a.depth[(uint64_t)kb * a.n + u] = val;
+    if ((bits >> kb) & 1ull) a.out[kb][u] = val;
   }
 }
 
@@ -126,7 +127,7 @@ __global__ void __launch_bounds__(kBlock) msbfs_persistent(Args a) {
     const uint32_t s = a.srcs[gtid];
     atomicOr(a.visit + s, 1ull << gtid);
     atomicOr(a.front[0] + s, 1ull << gtid);
-    a.depth[(uint64_t)gtid * a.n + s] = 0u;
+    a.out[gtid][s] = 0u;
     bool first = true;
     for (uint32_t j = 0; j < gtid; ++j) first &= a.srcs[j] != s;
     if (first) {
@@ -180,38 +181,73 @@ __global__ void __launch_bounds__(kBlock) msbfs_persistent(Args a) {
         while (mine) {
           const int kb = __ffsll((long long)mine) - 1;
           mine &= mine - 1;
-          a.depth[(uint64_t)kb * a.n + u] = val;
+          a.out[kb][u] = val;
         }
       }
     } else {
-      // phase A: pull -- every vertex missing bits ORs its in-neighbours' frontier words
+      // phase A: pull -- every vertex missing bits ORs its in-neighbours'
+      // frontier words.  A lane scans the first kPullLane in-edges of its
+      // vertex (four gathers in flight) and stops once no bit is missing;
+      // longer lists still missing bits are finished by the whole warp, one
+      // vertex at a time, 32 edges per step, so a high-degree vertex costs
+      // its warp deg/32 steps instead of deg serial loads on one lane.
       ++pull_levels;
       const uint32_t gw = gtid >> 5, nw = nthreads >> 5;
       for (uint32_t w = gw; w * 32 < a.n; w += nw) {
         const uint32_t u = w * 32 + lane;
-        unsigned long long bits = 0;
+        unsigned long long bits = 0, vis = a.full, accb = 0;
+        uint32_t rest_b = 0, rest_e = 0;
         if (u < a.n) {
-          const unsigned long long vis = __ldcg(a.visit + u);
+          vis = __ldcg(a.visit + u);
           if (vis != a.full) {
             const uint32_t b = __ldg(a.ioffs + u), e = __ldg(a.ioffs + u + 1);
-            unsigned long long accb = 0;
-            for (uint32_t x = b; x < e; ++x) {
-              accb |= __ldcg(fcur + __ldg(a.icols + x));
+            const uint32_t lim = min(e, b + kPullLane);
+            uint32_t x = b;
+            for (; x + 4 <= lim; x += 4) {
+              const uint32_t c0 = __ldg(a.icols + x), c1 = __ldg(a.icols + x + 1);
+              const uint32_t c2 = __ldg(a.icols + x + 2), c3 = __ldg(a.icols + x + 3);
+              accb |= __ldcg(fcur + c0) | __ldcg(fcur + c1) | __ldcg(fcur + c2) | __ldcg(fcur + c3);
               if ((accb | vis) == a.full) break;
             }
-            bits = accb & ~vis;
-            if (bits) {
-              acc[u] = bits;
-              a.visit[u] = vis | bits;
-              const uint32_t ob = __ldg(a.offs + u), oe = __ldg(a.offs + u + 1);
-              mf += oe - ob;
-              nbits += __popcll(bits);
-              const uint32_t pos = agg_reserve(&nx->tcount);
-              if (pos < a.cap) tnext[pos] = u;
-              if (!push_binned(u, ob, oe, a.huge, qnext, &nx->qcount, a.cap, cnext, &nx->ccount,
-                               a.chunk_cap))
-                atomicOr(a.err, kErrOverflow);
+            if ((accb | vis) != a.full) {
+              for (; x < lim; ++x) accb |= __ldcg(fcur + __ldg(a.icols + x));
+              if ((accb | vis) != a.full && e > lim) {
+                rest_b = lim;
+                rest_e = e;
+              }
             }
+          }
+        }
+        unsigned dm = __ballot_sync(0xffffffffu, rest_e > rest_b);
+        while (dm) {
+          const int sl = __ffs(dm) - 1;
+          dm &= dm - 1;
+          const uint32_t rb = __shfl_sync(0xffffffffu, rest_b, sl);
+          const uint32_t re = __shfl_sync(0xffffffffu, rest_e, sl);
+          const unsigned long long have =
+              __shfl_sync(0xffffffffu, accb | vis, sl);
+          unsigned long long wacc = 0;
+          for (uint32_t base = rb; base < re; base += 32) {
+            const uint32_t x = base + lane;
+            if (x < re) wacc |= __ldcg(fcur + __ldg(a.icols + x));
+            if ((warp_or64(wacc) | have) == a.full) break;
+          }
+          wacc = warp_or64(wacc);
+          if (lane == sl) accb |= wacc;
+        }
+        if (u < a.n && vis != a.full) {
+          bits = accb & ~vis;
+          if (bits) {
+            acc[u] = bits;
+            a.visit[u] = vis | bits;
+            const uint32_t ob = __ldg(a.offs + u), oe = __ldg(a.offs + u + 1);
+            mf += oe - ob;
+            nbits += __popcll(bits);
+            const uint32_t pos = agg_reserve(&nx->tcount);
+            if (pos < a.cap) tnext[pos] = u;
+            if (!push_binned(u, ob, oe, a.huge, qnext, &nx->qcount, a.cap, cnext, &nx->ccount,
+                             a.chunk_cap))
+              atomicOr(a.err, kErrOverflow);
           }
         }
         write_depths(a, u, bits, val);
@@ -326,35 +362,19 @@ int ws_get(grus_graph *g, Workspace **out) {
 }
 
 }  // namespace
-}  // namespace grus
 
-using namespace grus;
-
-extern "C" int grus_bfs_multi(grus_graph *g, const uint32_t *srcs, int k, uint32_t *depths,
-                              grus_stats *stats, void *stream) {
-  if (!g || !srcs || !depths || k < 1 || k > 64) return GRUS_EINVAL;
-  if (g->n == 0) return GRUS_EINVAL;
-  uint32_t hsrc[64];
-  GRUS_CUDA_TRY(cudaMemcpy(hsrc, srcs, k * 4, cudaMemcpyDefault));
+int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
+              grus_stats *stats, cudaStream_t s) {
+  if (!g || !hsrc || !outs || k < 1 || k > 64 || g->n == 0) return GRUS_EINVAL;
   for (int i = 0; i < k; ++i)
-    if (hsrc[i] >= g->n) {
+    if (hsrc[i] >= g->n || !outs[i]) {
       set_last_error("source vertex out of range");
       return GRUS_EINVAL;
     }
-  cudaStream_t s = (cudaStream_t)stream;
   std::lock_guard<std::mutex> lk(g->mu);
   Workspace *w = nullptr;
   int rc = ws_get(g, &w);
   if (rc) return rc;
-  const bool dev_out = is_device_pointer(depths);
-  const size_t out_bytes = (size_t)k * g->n * 4;
-  if (!dev_out && w->depth_bytes < out_bytes) {
-    cudaFree(w->depth);
-    w->depth = nullptr;
-    w->depth_bytes = 0;
-    GRUS_CUDA_TRY(cudaMalloc(&w->depth, out_bytes));
-    w->depth_bytes = out_bytes;
-  }
   static int occ = -1;
   if (occ < 0)
     GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, msbfs_persistent, kBlock, 0));
@@ -370,7 +390,7 @@ extern "C" int grus_bfs_multi(grus_graph *g, const uint32_t *srcs, int k, uint32
   a.m = g->m;
   a.k = k;
   a.srcs = w->srcs;
-  a.depth = dev_out ? depths : w->depth;
+  for (int i = 0; i < k; ++i) a.out[i] = outs[i];
   a.full = k == 64 ? ~0ull : ((1ull << k) - 1);
   a.visit = w->words;
   a.front[0] = w->words + g->n;
@@ -397,8 +417,7 @@ extern "C" int grus_bfs_multi(grus_graph *g, const uint32_t *srcs, int k, uint32
                          occ, s, nullptr, 0);
   if (rc) return rc;
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev1, s));
-  if (!dev_out) GRUS_CUDA_TRY(cudaMemcpyAsync(depths, w->depth, out_bytes, cudaMemcpyDeviceToHost, s));
-  if (!stats && dev_out) return GRUS_OK;
+  if (!stats) return GRUS_OK;
   GRUS_CUDA_TRY(cudaMemcpyAsync(w->ctrl_host, w->ctrl, kCtrlBytes, cudaMemcpyDeviceToHost, s));
   GRUS_CUDA_TRY(cudaStreamSynchronize(s));
   const uint32_t errbits = *(uint32_t *)(w->ctrl_host + kOffErr);
@@ -418,6 +437,49 @@ extern "C" int grus_bfs_multi(grus_graph *g, const uint32_t *srcs, int k, uint32
     float ms = 0.f;
     cudaEventElapsedTime(&ms, w->ev0, w->ev1);
     stats->device_ms = ms;
+  }
+  return GRUS_OK;
+}
+
+}  // namespace grus
+
+using namespace grus;
+
+extern "C" int grus_bfs_multi(grus_graph *g, const uint32_t *srcs, int k, uint32_t *depths,
+                              grus_stats *stats, void *stream) {
+  if (!g || !srcs || !depths || k < 1 || k > 64) return GRUS_EINVAL;
+  if (g->n == 0) return GRUS_EINVAL;
+  uint32_t hsrc[64];
+  GRUS_CUDA_TRY(cudaMemcpy(hsrc, srcs, k * 4, cudaMemcpyDefault));
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool dev_out = is_device_pointer(depths);
+  const size_t out_bytes = (size_t)k * g->n * 4;
+  uint32_t *base = depths;
+  if (!dev_out) {
+    Workspace *w = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(g->mu);
+      int rc = ws_get(g, &w);
+      if (rc) return rc;
+      if (w->depth_bytes < out_bytes) {
+        cudaFree(w->depth);
+        w->depth = nullptr;
+        w->depth_bytes = 0;
+        GRUS_CUDA_TRY(cudaMalloc(&w->depth, out_bytes));
+        w->depth_bytes = out_bytes;
+      }
+    }
+    base = w->depth;
+  }
+  uint32_t *outs[64];
+  for (int i = 0; i < k; ++i) outs[i] = base + (size_t)i * g->n;
+  grus_stats local;
+  // a host output is copied back after the launch: wait for it and check errors
+  int rc = msbfs_run(g, hsrc, k, outs, stats ? stats : (dev_out ? nullptr : &local), s);
+  if (rc) return rc;
+  if (!dev_out) {
+    GRUS_CUDA_TRY(cudaMemcpyAsync(depths, base, out_bytes, cudaMemcpyDeviceToHost, s));
+    GRUS_CUDA_TRY(cudaStreamSynchronize(s));
   }
   return GRUS_OK;
 }

@@ -1,15 +1,24 @@
 // serve.cu -- a query server over device-resident graphs (continuous batching).
 //
 // Requests (graph, BFS|SSSP, source, device output) are queued by
-// grus_server_submit from any host thread.  A scheduler thread admits them
-// into worker slots: a slot is one cluster worker of the batch engine
-// (batch.cu) with its own per-query device state and CUDA stream.  A slot's
-// state is allocated the first time it is used, and only if free HBM
-// (cudaMemGetInfo) covers it plus a reserve -- admission by free HBM.  Each
-// admitted query is one single-worker launch on its slot's stream, so queries
-// that arrive while others run start as soon as a slot is free and overlap on
-// the device.  Completion is observed with an event per slot; latency is
-// completion time minus submission time on the host clock.
+// grus_server_submit from any host thread and served by two lanes.
+//   Small graphs: a scheduler thread admits each request into a worker slot:
+//     one cluster worker of the batch engine (batch.cu) with its own
+//     per-query device state and CUDA stream.  A slot's state is allocated the
+//     first time it is used, and only if free HBM (cudaMemGetInfo) covers it
+//     plus a reserve -- admission by free HBM.  Each admitted query is one
+//     single-worker launch on its slot's stream, so queries that arrive while
+//     others run start as soon as a slot is free and overlap on the device.
+//   Big graphs (at least big_edges edges): one cluster would take many times
+//     longer than the whole GPU, so a second thread runs the whole-GPU
+//     persistent kernels (grus_bfs / grus_sssp) one launch at a time, and
+//     packs every queued BFS request on the same graph -- up to 64 -- into one
+//     multi-source launch (msbfs.cu) that writes each request's own output.
+//     A graph's workspace is allocated only if free HBM covers it plus the
+//     reserve.
+// Completion is observed with an event per slot (small lane) or when the
+// whole-GPU call returns (big lane); latency is completion time minus
+// submission time on the host clock.
 // The reference has no serving path (one query per process run).
 #include <algorithm>
 #include <atomic>
@@ -54,17 +63,22 @@ struct Slot {
 
 struct grus_server {
   std::vector<grus_graph *> graphs;
+  std::vector<uint8_t> big;  // per graph: served by the whole-GPU lane
   grus::GraphDesc *d_graphs = nullptr;
-  uint64_t max_n = 0, max_m = 0;
+  uint64_t max_n = 0, max_m = 0;  // over the small graphs
+  uint64_t big_edges = 1ull << 24;
   int cluster = 8;
   uint32_t huge = 8192, delta = 96;
   uint64_t reserve = 1ull << 30;
   std::vector<grus::Slot> slots;
   std::mutex mu;
   std::condition_variable cv;
-  std::deque<grus::Request> pending;
+  std::deque<grus::Request> pending;      // small lane
+  std::deque<grus::Request> big_pending;  // big lane
   std::deque<grus_completion> completed;
-  std::thread worker;
+  std::thread worker, big_worker;
+  cudaStream_t big_stream = nullptr;
+  uint64_t big_launches = 0, big_queries = 0;
   std::atomic<bool> stop{false};
   int device = 0;
   uint64_t admitted = 0, finished = 0, rejected = 0;
@@ -201,6 +215,94 @@ void scheduler(grus_server *s) {
   }
 }
 
+// Rough device bytes of a graph's whole-GPU workspace for `algo` (BFS also
+// covers the multi-source one), used for admission before the first launch.
+size_t big_workspace_bytes(const grus_graph *g, uint32_t algo) {
+  const size_t n = g->n, m = g->m;
+  return (algo == GRUS_ALGO_SSSP ? 20 * n : 40 * n) + m / 32 + (1u << 20);
+}
+
+bool big_workspace_ready(const grus_graph *g, uint32_t algo, bool multi) {
+  if (algo == GRUS_ALGO_SSSP) return g->ws[kWsSssp] != nullptr;
+  return multi ? g->ws[kWsMsBfs] != nullptr : g->ws[kWsBfs] != nullptr;
+}
+
+void complete(grus_server *s, const Request &r, int status, Clock::time_point now) {
+  grus_completion c;
+  std::memset(&c, 0, sizeof(c));
+  c.tag = r.tag;
+  c.status = status;
+  c.latency_us = std::chrono::duration<double, std::micro>(now - r.t_submit).count();
+  s->completed.push_back(c);
+  ++s->finished;
+}
+
+void big_scheduler(grus_server *s) {
+  cudaSetDevice(s->device);
+  std::vector<Request> group;
+  group.reserve(64);
+  while (true) {
+    group.clear();
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv.wait_for(lk, std::chrono::milliseconds(50),
+                     [&] { return s->stop.load() || !s->big_pending.empty(); });
+      if (s->stop.load()) return;
+      if (s->big_pending.empty()) continue;
+      const Request first = s->big_pending.front();
+      s->big_pending.pop_front();
+      group.push_back(first);
+      if (first.algo == GRUS_ALGO_BFS) {
+        for (auto it = s->big_pending.begin(); it != s->big_pending.end() && group.size() < 64;) {
+          if (it->graph == first.graph && it->algo == GRUS_ALGO_BFS) {
+            group.push_back(*it);
+            it = s->big_pending.erase(it);
+          } else {
+            ++it;
+          }
+        }
+      }
+    }
+    const Request &r = group[0];
+    grus_graph *g = s->graphs[r.graph];
+    const bool multi = group.size() > 1;
+    int rc = GRUS_OK;
+    if (!big_workspace_ready(g, r.algo, multi)) {
+      size_t free_b = 0, total_b = 0;
+      const cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+      if (e != cudaSuccess) rc = status_from_cuda(e);
+      else if (free_b < big_workspace_bytes(g, r.algo) + s->reserve) rc = GRUS_ENOMEM;
+    }
+    if (rc == GRUS_OK) {
+      grus_stats st;  // a stats call waits for the launch and checks its error word
+      if (r.algo == GRUS_ALGO_SSSP) {
+        rc = grus_sssp(g, r.src, r.out, &st, s->big_stream);
+      } else if (!multi) {
+        rc = grus_bfs(g, r.src, r.out, &st, s->big_stream);
+      } else {
+        uint32_t srcs[64];
+        uint32_t *outs[64];
+        for (size_t i = 0; i < group.size(); ++i) {
+          srcs[i] = group[i].src;
+          outs[i] = group[i].out;
+        }
+        rc = msbfs_run(g, srcs, (int)group.size(), outs, &st, s->big_stream);
+      }
+    }
+    const auto now = Clock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (rc == GRUS_ENOMEM) {
+      s->rejected += group.size();
+    } else {
+      ++s->big_launches;
+      s->big_queries += group.size();
+      s->admitted += group.size();
+    }
+    for (const Request &q : group) complete(s, q, rc, now);
+    s->cv.notify_all();
+  }
+}
+
 }  // namespace
 }  // namespace grus
 
@@ -214,6 +316,15 @@ int grus_server_create(grus_graph *const *graphs, int ngraphs, const grus_server
   grus_server *s = new grus_server();
   cudaGetDevice(&s->device);
   std::vector<GraphDesc> descs;
+  int nslots = 16;
+  if (cfg) {
+    if (cfg->slots) nslots = (int)cfg->slots;
+    if (cfg->cluster_size) s->cluster = (int)cfg->cluster_size;
+    if (cfg->hbm_reserve_bytes) s->reserve = cfg->hbm_reserve_bytes;
+    if (cfg->sssp_delta) s->delta = cfg->sssp_delta;
+    if (cfg->big_edges) s->big_edges = cfg->big_edges == 0xFFFFFFFFu ? ~0ull : cfg->big_edges;
+  }
+  bool any_small = false;
   for (int i = 0; i < ngraphs; ++i) {
     if (!graphs[i]) {
       delete s;
@@ -221,15 +332,13 @@ int grus_server_create(grus_graph *const *graphs, int ngraphs, const grus_server
     }
     s->graphs.push_back(graphs[i]);
     descs.push_back(describe(graphs[i]));
-    s->max_n = std::max<uint64_t>(s->max_n, graphs[i]->n);
-    s->max_m = std::max<uint64_t>(s->max_m, graphs[i]->m);
-  }
-  int nslots = 16;
-  if (cfg) {
-    if (cfg->slots) nslots = (int)cfg->slots;
-    if (cfg->cluster_size) s->cluster = (int)cfg->cluster_size;
-    if (cfg->hbm_reserve_bytes) s->reserve = cfg->hbm_reserve_bytes;
-    if (cfg->sssp_delta) s->delta = cfg->sssp_delta;
+    const bool big = graphs[i]->m >= s->big_edges;
+    s->big.push_back(big ? 1 : 0);
+    if (!big) {
+      any_small = true;
+      s->max_n = std::max<uint64_t>(s->max_n, graphs[i]->n);
+      s->max_m = std::max<uint64_t>(s->max_m, graphs[i]->m);
+    }
   }
   if (s->cluster < 1 || s->cluster > 16 || nslots < 1 || nslots > 1024) {
     delete s;
@@ -237,7 +346,7 @@ int grus_server_create(grus_graph *const *graphs, int ngraphs, const grus_server
   }
   s->slots.resize(nslots);
   int probe_workers = 0;
-  if (batch_occupancy(s->cluster, &probe_workers) != GRUS_OK || probe_workers < 1) {
+  if (any_small && (batch_occupancy(s->cluster, &probe_workers) != GRUS_OK || probe_workers < 1)) {
     delete s;
     set_last_error("server: no cluster of this size can be resident");
     return GRUS_EINVAL;
@@ -251,7 +360,15 @@ int grus_server_create(grus_graph *const *graphs, int ngraphs, const grus_server
     set_last_error(cudaGetErrorString(e));
     return status_from_cuda(e);
   }
+  e = cudaStreamCreateWithFlags(&s->big_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    cudaFree(s->d_graphs);
+    delete s;
+    set_last_error(cudaGetErrorString(e));
+    return status_from_cuda(e);
+  }
   s->worker = std::thread(scheduler, s);
+  s->big_worker = std::thread(big_scheduler, s);
   *out = s;
   return GRUS_OK;
 }
@@ -270,7 +387,7 @@ int grus_server_submit(grus_server *s, uint32_t graph, uint32_t algo, uint32_t s
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->error) return s->error;
-    s->pending.push_back(r);
+    (s->big[graph] ? s->big_pending : s->pending).push_back(r);
   }
   s->cv.notify_all();
   return GRUS_OK;
@@ -293,10 +410,12 @@ int grus_server_get_stats(grus_server *s, grus_server_stats *st) {
   if (!s || !st) return GRUS_EINVAL;
   std::lock_guard<std::mutex> lk(s->mu);
   std::memset(st, 0, sizeof(*st));
-  st->submitted = s->admitted + s->pending.size();
+  st->pending = s->pending.size() + s->big_pending.size();
+  st->submitted = s->admitted + s->rejected + st->pending;
   st->admitted = s->admitted;
   st->completed = s->finished;
-  st->pending = s->pending.size();
+  st->big_launches = s->big_launches;
+  st->big_queries = s->big_queries;
   st->slots_ready = (uint32_t)s->slots_ready;
   st->rejected = s->rejected;
   st->slots = (uint32_t)s->slots.size();
@@ -308,6 +427,11 @@ int grus_server_destroy(grus_server *s) {
   s->stop.store(true);
   s->cv.notify_all();
   if (s->worker.joinable()) s->worker.join();
+  if (s->big_worker.joinable()) s->big_worker.join();
+  if (s->big_stream) {
+    cudaStreamSynchronize(s->big_stream);
+    cudaStreamDestroy(s->big_stream);
+  }
   for (auto &sl : s->slots) {
     if (sl.stream) cudaStreamSynchronize(sl.stream);
     sl.state.release();

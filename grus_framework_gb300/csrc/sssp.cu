@@ -51,6 +51,14 @@ struct Summary {
   unsigned long long visits, nr, mr;
 };
 
+// Per-level record: end time, relaxations, frontier size (queue entries +
+// hub chunks) and the number of threshold advances so far.
+constexpr int kMaxTrace = 256;
+struct LevelTrace {
+  unsigned long long t_ns, visits;
+  uint32_t frontier, splits;
+};
+
 struct Args {
   const uint32_t *__restrict__ offs;
   const uint32_t *__restrict__ cols;
@@ -69,6 +77,7 @@ struct Args {
   GridBarrier *bar;
   uint32_t *err;
   Summary *summary;
+  LevelTrace *trace;
   uint32_t delta, huge;
   uint64_t timeout_ns;
 };
@@ -83,6 +92,8 @@ struct Workspace {
   uint4 *chunks = nullptr;
   uint32_t chunk_cap = 0;
   char *ctrl = nullptr, *ctrl_host = nullptr;
+  LevelTrace *trace = nullptr, *trace_host = nullptr;
+  int trace_levels = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -98,7 +109,9 @@ void ws_free(void *p) {
   cudaFree(w->far);
   cudaFree(w->chunks);
   cudaFree(w->ctrl);
+  cudaFree(w->trace);
   if (w->ctrl_host) cudaFreeHost(w->ctrl_host);
+  if (w->trace_host) cudaFreeHost(w->trace_host);
   if (w->ev0) cudaEventDestroy(w->ev0);
   if (w->ev1) cudaEventDestroy(w->ev1);
   delete w;
@@ -123,6 +136,8 @@ int ws_get(grus_graph *g, Workspace **out) {
   if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
   if (e == cudaSuccess) e = cudaMemset(w->ctrl, 0, kCtrlBytes);
   if (e == cudaSuccess) e = cudaMallocHost(&w->ctrl_host, kCtrlBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&w->trace, kMaxTrace * sizeof(LevelTrace));
+  if (e == cudaSuccess) e = cudaMallocHost(&w->trace_host, kMaxTrace * sizeof(LevelTrace));
   if (e == cudaSuccess) e = cudaEventCreate(&w->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&w->ev1);
   if (e != cudaSuccess) {
@@ -203,6 +218,7 @@ __global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
 
   uint32_t L = 0, T = a.delta, fsel = 0, splits = 0;
   unsigned long long visits = 0;
+  if (gtid == 0 && a.trace) a.trace[0] = LevelTrace{global_timer_ns(), 0ull, 1u, 0u};
   while (true) {
     Slot *cur = a.slots + (L & 3u), *nx = a.slots + ((L + 1) & 3u);
     uint32_t *inq_next = a.inq[(L + 1) % 3];
@@ -217,7 +233,8 @@ __global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
     const unsigned long long bv = block_sum_u64<kBlock>(vis.visits);
     if (threadIdx.x == 0 && bv) atomicAdd(&nx->visits, bv);
     if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-    visits += __ldcg(&nx->visits);
+    const unsigned long long lv = __ldcg(&nx->visits);
+    visits += lv;
     ++L;
     bool done = false;
     // near frontier empty: advance the threshold and split the far pile
@@ -263,6 +280,8 @@ __global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
       ++splits;
       if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
     }
+    if (gtid == 0 && a.trace && L < (uint32_t)kMaxTrace)
+      a.trace[L] = LevelTrace{global_timer_ns(), lv, qc + cc, splits};
     if (done) break;
     if (L > 4u * a.n + 64u) {
       if (gtid == 0) atomicOr(a.err, kErrLevels);
@@ -341,6 +360,7 @@ extern "C" int grus_sssp(grus_graph *g, uint32_t src, uint32_t *dist,
   a.bar = (GridBarrier *)(w->ctrl + kOffBar);
   a.err = (uint32_t *)(w->ctrl + kOffErr);
   a.summary = (Summary *)(w->ctrl + kOffSummary);
+  a.trace = stats ? w->trace : nullptr;
   a.delta = std::max(1u, tune_or(g->tuning.sssp_delta, kDefDelta));
   a.huge = tune_or(g->tuning.huge_degree, kDefHuge);
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
@@ -365,6 +385,9 @@ extern "C" int grus_sssp(grus_graph *g, uint32_t src, uint32_t *dist,
   }
   if (stats) {
     const Summary *sm = (const Summary *)(w->ctrl_host + kOffSummary);
+    GRUS_CUDA_TRY(cudaMemcpy(w->trace_host, w->trace, kMaxTrace * sizeof(LevelTrace),
+                             cudaMemcpyDeviceToHost));
+    w->trace_levels = std::min<int>((int)sm->levels + 1, kMaxTrace);
     std::memset(stats, 0, sizeof(*stats));
     stats->levels = sm->levels;
     stats->direction_switches = sm->splits;  // threshold advances
@@ -377,4 +400,21 @@ extern "C" int grus_sssp(grus_graph *g, uint32_t src, uint32_t *dist,
     stats->device_ms = ms;
   }
   return GRUS_OK;
+}
+
+extern "C" int grus_sssp_trace(grus_graph *g, grus_level_trace *out, int max_levels) {
+  if (!g || (!out && max_levels > 0) || max_levels < 0) return GRUS_EINVAL;
+  std::lock_guard<std::mutex> lk(g->mu);
+  const Workspace *w = (const Workspace *)g->ws[kWsSssp];
+  if (!w || w->trace_levels < 2) return 0;
+  const int levels = std::min(w->trace_levels - 1, max_levels);
+  const uint64_t t0 = w->trace_host[0].t_ns;
+  for (int i = 0; i < levels; ++i) {
+    const LevelTrace &r = w->trace_host[i + 1];
+    out[i].end_ns = r.t_ns - t0;
+    out[i].edges = r.visits;
+    out[i].vertices = r.frontier;
+    out[i].pull = r.splits;
+  }
+  return levels;
 }

@@ -183,6 +183,10 @@ typedef struct grus_level_trace {
 } grus_level_trace;
 /* Copies up to max_levels records; returns how many (>= 0) or a status. */
 GRUS_API int grus_bfs_trace(grus_graph *g, grus_level_trace *out, int max_levels);
+/* Per-level records of the last grus_sssp call on g made with stats: end
+ * time, relaxations (edges), frontier entries (vertices) and the number of
+ * threshold advances so far (pull).  Same return convention. */
+GRUS_API int grus_sssp_trace(grus_graph *g, grus_level_trace *out, int max_levels);
 
 /* Allocation-free BFS.  No counterpart in the reference.  For callers that
  * cannot allocate device memory (a host process that owns the whole device
@@ -269,12 +273,17 @@ GRUS_API int grus_batch_get_info(const grus_batch *b, grus_batch_config *info);
 GRUS_API int grus_batch_free(grus_batch *b);
 
 /* ---- serving --------------------------------------------------------------- */
-/* A query server over device-resident graphs.  Requests queue on the host; a
- * scheduler thread admits each into a worker slot (one cluster worker of the
- * batch engine with its own device state and stream) as soon as a slot is
- * free, allocating a slot's state only if free HBM covers it plus
- * hbm_reserve_bytes.  Admitted queries overlap on the device.  Latency is
- * measured from submit to observed completion on the host clock. */
+/* A query server over device-resident graphs.  Requests queue on the host
+ * and are served by two lanes.  Small graphs (fewer than big_edges edges): a
+ * scheduler thread admits each query into a worker slot (one cluster worker
+ * of the batch engine with its own device state and stream) as soon as a slot
+ * is free, allocating a slot's state only if free HBM covers it plus
+ * hbm_reserve_bytes; admitted queries overlap on the device.  Big graphs: a
+ * second thread runs whole-GPU persistent launches one at a time, and packs
+ * every queued BFS query on the same graph (up to 64) into one multi-source
+ * launch; a graph's workspace is allocated only if free HBM covers it plus
+ * the reserve.  Latency is measured from submit to observed completion on the
+ * host clock. */
 typedef struct grus_server grus_server;
 
 typedef struct grus_server_config {
@@ -282,7 +291,8 @@ typedef struct grus_server_config {
   uint32_t cluster_size;     /* CTAs per query (1..16, default 8) */
   uint64_t hbm_reserve_bytes;/* free HBM kept back at admission (default 1 GiB) */
   uint32_t sssp_delta;
-  uint32_t reserved;
+  uint32_t big_edges;        /* graphs with at least this many edges run on the
+                                whole-GPU lane (default 2^24; 0xFFFFFFFF: never) */
 } grus_server_config;
 
 typedef struct grus_completion {
@@ -295,6 +305,9 @@ typedef struct grus_completion {
 typedef struct grus_server_stats {
   uint64_t submitted, admitted, completed, pending, rejected;
   uint32_t slots, slots_ready;
+  uint64_t big_launches;     /* whole-GPU launches of the big-graph lane */
+  uint64_t big_queries;      /* queries they served (BFS queries on one graph
+                                share a multi-source launch) */
 } grus_server_stats;
 
 GRUS_API int grus_server_create(grus_graph *const *graphs, int ngraphs,

@@ -65,3 +65,45 @@ def test_server_rejects_bad_submissions(grus, graphs):
     with pytest.raises(grus.GrusError):
         srv.submit(0, grus.ALGO_BFS, 0, host, 0)
     srv.close()
+
+
+def test_server_big_lane_groups_bfs_and_matches_alone(grus, graphs):
+    """With big_edges=1 every graph is served by the whole-GPU lane: queued BFS
+    queries on one graph share multi-source launches, SSSP runs alone, and each
+    result equals the query run alone."""
+    torch = pytest.importorskip("torch")
+    srv = grus.Server(graphs, slots=2, big_edges=1)
+    rng = np.random.default_rng(7)
+    reqs, outs = [], []
+    for tag in range(150):
+        gi = int(rng.integers(len(graphs)))
+        algo = grus.ALGO_BFS if tag % 5 else grus.ALGO_SSSP
+        src = int(rng.integers(graphs[gi].n))
+        out = torch.empty(graphs[gi].n, dtype=torch.int32, device="cuda")
+        reqs.append((gi, algo, src))
+        outs.append(out)
+        srv.submit(gi, algo, src, out, tag)
+    done = drain(srv, len(reqs))
+    assert len(done) == len(reqs)
+    assert all(st == 0 for st, _ in done.values())
+    for (gi, algo, src), out in zip(reqs, outs):
+        alone = grus.sssp(graphs[gi], src) if algo == grus.ALGO_SSSP else grus.bfs(graphs[gi], src)
+        assert np.array_equal(out.cpu().numpy().view(np.uint32), alone)
+    st = srv.stats()
+    assert st["big_queries"] == len(reqs) and st["completed"] == len(reqs)
+    assert st["big_launches"] < len(reqs)  # BFS queries were packed
+    srv.close()
+
+
+def test_server_big_lane_admission_by_free_hbm(grus):
+    """A fresh graph whose whole-GPU workspace does not fit under the reserve is refused."""
+    torch = pytest.importorskip("torch")
+    g = grus.Graph.rmat(11, 8, 71, symmetric=True, weighted=True)
+    srv = grus.Server([g], slots=2, big_edges=1, hbm_reserve_bytes=1 << 50)
+    out = torch.empty(g.n, dtype=torch.int32, device="cuda")
+    srv.submit(0, grus.ALGO_SSSP, 0, out, 3)
+    done = drain(srv, 1, timeout=30)
+    assert done[3][0] == grus.ENOMEM
+    assert srv.stats()["rejected"] == 1
+    srv.close()
+    g.free()
