@@ -277,7 +277,7 @@ __device__ void run_sssp(const Args &a, const Ctx &c, cg::cluster_group &cl, con
   cl.sync();
 }
 
-__global__ void __launch_bounds__(kBatchBlock) batch_kernel(Args a) {
+__global__ void __launch_bounds__(kBatchBlock, 4) batch_kernel(Args a) {
   cg::cluster_group cl = cg::this_cluster();
   __shared__ uint32_t s_task;
   Ctx c;
@@ -456,7 +456,7 @@ struct grus_batch {
   uint32_t task_cap = 0;
   grus::BatchState state;
   int cluster = 16, workers = 0;
-  uint32_t huge = 8192, delta = 96;
+  uint32_t huge = 1024, delta = 96;
   uint64_t max_n = 0, max_m = 0, total_out = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;

@@ -14,7 +14,7 @@
 //     4 * n/8 bytes, one contiguous block covered by an L2 persistence window)
 //     and a vertex queue for push levels.
 //   * push (top-down) levels, degree-binned:
-//       - degree >= huge (8192): split into 4096-edge chunks when enqueued,
+//       - degree >= huge (8192): split into 1024-edge chunks when enqueued,
 //         each chunk expanded by a whole CTA (spreads hubs over all SMs);
 //       - degree >= 256: CTA-cooperative expansion within a queue tile;
 //       - degree >= 32: warp-cooperative expansion;

@@ -32,7 +32,7 @@ namespace {
 constexpr int kBlock = 256;
 constexpr uint32_t kSample = 2;
 constexpr int kModeSamples = 1024;
-constexpr uint32_t kDefHuge = 8192;
+constexpr uint32_t kDefHuge = 1024;
 
 __device__ __forceinline__ uint32_t find_root(uint32_t *p, uint32_t x) {
   uint32_t y = __ldcg(p + x);

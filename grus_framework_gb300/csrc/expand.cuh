@@ -134,18 +134,24 @@ __device__ __forceinline__ void expand_chunks(const uint4 *ccur, uint32_t ccount
   expand_chunks<kBlock>(ccur, ccount, vis, blockIdx.x, gridDim.x);
 }
 
-// Expands the queue tile-by-tile, then the chunk list.  Must be called by
-// every thread of the CTA.
+// Expands the queue tile by tile, then the chunk list.  A tile holds
+// min(256, ceil(qcount / parts)) entries and tiles are dealt to the CTAs in
+// turn, so a small frontier of heavy vertices spreads over as many CTAs as it
+// has vertices (whole 256-entry tiles would put a 44-vertex frontier of
+// degree-750 vertices on one CTA), while large frontiers keep full tiles.
+// Must be called by every thread of the CTA.
 template <int kBlock, class Visitor>
 __device__ __forceinline__ void expand_binned(const uint32_t *__restrict__ offs,
                                               const uint32_t *qcur, uint32_t qcount,
                                               const uint4 *ccur, uint32_t ccount,
                                               Visitor &vis, uint32_t part, uint32_t parts) {
-  for (uint32_t base = part * kBlock; base < qcount; base += parts * kBlock) {
+  const uint32_t tile = min((uint32_t)kBlock, qcount / parts + (qcount % parts != 0));
+  for (uint32_t base = part * tile; base < qcount; base += parts * tile) {
     const uint32_t i = base + threadIdx.x;
+    const uint32_t hi = min(base + tile, qcount);
     uint32_t v = 0, beg = 0, end = 0;
     typename Visitor::aux_t aux{};
-    if (i < qcount) {
+    if (i < hi) {
       v = __ldcg(qcur + i);
       beg = __ldg(offs + v);
       end = __ldg(offs + v + 1);

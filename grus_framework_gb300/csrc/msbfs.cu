@@ -29,7 +29,7 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr uint32_t kPullLane = 32;  // in-edges a lane scans alone in a pull level
-constexpr uint32_t kDefHuge = 8192;
+constexpr uint32_t kDefHuge = 1024;
 constexpr float kDefAlpha = 15.f;
 
 struct Slot {

@@ -29,7 +29,7 @@ namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr uint32_t kDefHuge = 8192;
+constexpr uint32_t kDefHuge = 1024;
 constexpr uint32_t kDefDelta = 96;
 
 struct Slot {
