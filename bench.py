@@ -10,7 +10,8 @@ the device from the seed.
 
 A step is one query over the resident graph.  Metric: GTEPS = traversed
 edges / time (BFS/SSSP: m_r = sum of out-degrees of reached vertices; CC: m;
-PageRank: m x iterations; 64-source BFS: the sum of m_r over the sources).
+PageRank: m x iterations; multi-source BFS/SSSP: the sum of m_r over the
+sources).
 `value` is timed with CUDA events on the launching stream (device-resident
 input and output); `e2e` is the same query through the public API with a
 pinned HOST output buffer (the result is copied back inside the timed
@@ -21,7 +22,8 @@ events.
                   [--workload NAME] [--scale S]
 
 Other workloads (`--workload`): sssp-rmat22, cc-rmat22, pagerank-rmat24
-(directed), bfs-grid4096, msbfs-rmat23 (64 sources).  `--scale` overrides
+(directed), bfs-grid4096, msbfs-rmat23 (64 sources), msssp-rmat22 (32
+sources).  `--scale` overrides
 the RMAT scale (or the grid side as a power of two) for small profiling runs.
 
 `--impl reference` times the CPU path (the reference has no host traversal;
@@ -68,6 +70,9 @@ WORKLOADS = {
     "msbfs-rmat23": dict(algo="msbfs", graph="rmat", scale=23, edge_factor=16, seed=4,
                          symmetric=True, weighted=False, kernel="msbfs_persistent", sources=64,
                          metric="GTEPS (64-source BFS in one launch, RMAT-23 symmetrised)"),
+    "msssp-rmat22": dict(algo="msssp", graph="rmat", scale=22, edge_factor=16, seed=2,
+                         symmetric=True, weighted=True, kernel="msssp_persistent", sources=32,
+                         metric="GTEPS (32-source SSSP in one launch, RMAT-22 symmetrised, w in [1,255])"),
 }
 DEFAULT_WORKLOAD = "bfs-rmat24"
 
@@ -89,7 +94,9 @@ def alg_bytes(algo, n, m, nr, mr, iters=1, sources=1):
     sssp: as bfs with 8 m_r (column id + weight per relaxed edge);
     cc:   4(n+1) + 4m + 8n (labels read and written once);
     pagerank: per iteration 4(n+1) + 8m (column id + contribution) + 8n;
-    msbfs: 4(n+1) + 4m + 8n (visit/frontier words) + 4 * sources * n depths.
+    msbfs: 4(n+1) + 4m + 8n (visit/frontier words) + 4 * sources * n depths;
+    msssp: 4(n+1) + 8m (column id + weight, read once for all sources) +
+           8 * sources * n (distance matrix initialised once, outputs written once).
     """
     if algo == "bfs":
         return 4 * (n + 1) + 4 * mr + 4 * n + 8 * nr
@@ -101,6 +108,8 @@ def alg_bytes(algo, n, m, nr, mr, iters=1, sources=1):
         return iters * (4 * (n + 1) + 8 * m + 8 * n)
     if algo == "msbfs":
         return 4 * (n + 1) + 4 * m + 8 * n + 4 * sources * n
+    if algo == "msssp":
+        return 4 * (n + 1) + 8 * m + 8 * sources * n
     raise ValueError(algo)
 
 
@@ -256,14 +265,16 @@ def cpu_run(w, csr, csc, src, srcs, threads, budget_s=12.0, max_runs=5):
         while len(times) < max_runs and (not times or time.perf_counter() - t_start < budget_s):
             times.append(oracle.omp_pagerank(csc, outdeg, 0.85, it, threads)[1])
         desc = f"{len(times)} runs of {it} pull iterations"
-    elif algo == "msbfs":
+    elif algo in ("msbfs", "msssp"):
+        fn = oracle.omp_bfs if algo == "msbfs" else oracle.omp_sssp
         per = []
-        for s in srcs[:4]:  # bounded sample: 4 of the 64 sources, one BFS each
-            d, t = oracle.omp_bfs(csr, int(s), threads)
+        for s in srcs[:4]:  # bounded sample: 4 of the sources, one run each
+            d, t = fn(csr, int(s), threads)
             per.append((oracle.reached_edges(csr, d), t))
         units = sum(p[0] for p in per)
         times = [sum(p[1] for p in per)]
-        desc = "one OpenMP BFS from each of the first 4 of the 64 sources"
+        desc = (f"one OpenMP {'BFS' if algo == 'msbfs' else 'SSSP'} from each of the first 4 "
+                f"of the {len(srcs)} sources")
     med = statistics.median(times)
     return units / med / 1e9, f"{desc}, median {med*1e3:.1f} ms, OpenMP level-synchronous"
 
@@ -302,8 +313,7 @@ def run_grus(args, dist, rank, local):
     srcs = None
     iters = w.get("iters", 1)
     k = w.get("sources", 1)
-    if algo == "msbfs":
-        offs_h = None
+    if algo in ("msbfs", "msssp"):
         offs_h, _, _ = g.copy_csr()
         srcs = msbfs_sources(n, lambda v: int(offs_h[v + 1]) - int(offs_h[v]), k, 4)
         del offs_h
@@ -311,7 +321,7 @@ def run_grus(args, dist, rank, local):
         g.build_csc()
 
     def make_out(host):
-        shape = (k, n) if algo == "msbfs" else (n,)
+        shape = (k, n) if algo in ("msbfs", "msssp") else (n,)
         dt = torch.float32 if algo == "pagerank" else torch.int32
         if host:
             return torch.empty(shape, dtype=dt, pin_memory=True)
@@ -326,13 +336,15 @@ def run_grus(args, dist, rank, local):
             return grus.cc(g, out=out, stream=stream, stats=stats)
         if algo == "pagerank":
             return grus.pagerank(g, 0.85, iters, out=out, stream=stream, stats=stats)
+        if algo == "msssp":
+            return grus.sssp_multi(g, srcs, out=out, stream=stream, stats=stats)
         return grus.bfs_multi(g, srcs, out=out, stream=stream, stats=stats)
 
     out_dev = make_out(False)
     _, st = call(out_dev, stats=True)
     nr, mr = st["vertices_reached"], st["edges_reached"]
     launches = max(int(st["kernel_launches"]), 1)
-    units = {"bfs": mr, "sssp": mr, "cc": m, "pagerank": m * iters, "msbfs": mr}[algo]
+    units = {"bfs": mr, "sssp": mr, "cc": m, "pagerank": m * iters, "msbfs": mr, "msssp": mr}[algo]
     for _ in range(args.warmup):
         call(out_dev)
     torch.cuda.synchronize()
@@ -370,14 +382,14 @@ def run_grus(args, dist, rank, local):
     e2e_total = reduce_max(dist, sum(e2e_s))
     e2e_value = total_units / e2e_total / 1e9
     d2h = out_host.numel() * 4
-    h2d = 4 * (k if algo == "msbfs" else (1 if algo in ("bfs", "sssp") else 0))
+    h2d = 4 * (k if algo in ("msbfs", "msssp") else (1 if algo in ("bfs", "sssp") else 0))
 
     # cheap checks of the timed configuration (full parity lives in tests/)
     res = out_host.numpy()
     if algo in ("bfs", "sssp"):
         d = res.view(np.uint32)
         assert d[src] == 0 and int(np.count_nonzero(d != INFINIT)) == nr
-    elif algo == "msbfs":
+    elif algo in ("msbfs", "msssp"):
         d = res.view(np.uint32)
         assert all(d[i, s] == 0 for i, s in enumerate(srcs))
     elif algo == "cc":
@@ -412,7 +424,7 @@ def run_grus(args, dist, rank, local):
                    "sample": sample}
         clocks = clk.summary()
         cfg = {k_: v_ for k_, v_ in w.items() if k_ not in ("metric", "kernel")}
-        cfg.update({"n": n, "m": m, "src": src if algo != "msbfs" else "64 seeded (seed 4)",
+        cfg.update({"n": n, "m": m, "src": src if algo not in ("msbfs", "msssp") else f"{k} seeded (seed 4)",
                     "l2": "flushed (256 MB write) before each step",
                     "parallelism": f"replicas x{ws}", "levels": st["levels"],
                     "bottom_up_levels": st["bottom_up_levels"],
@@ -450,8 +462,8 @@ def run_reference(args, dist, rank):
     src = grid_source(1 << w["scale"]) if w["graph"] == "grid" else oracle.max_degree_vertex(g)
     csc = oracle.csr_to_csc(g) if algo == "pagerank" else None
     srcs = None
-    if algo == "msbfs":
-        srcs = msbfs_sources(g.n, lambda v: int(g.offs[v + 1]) - int(g.offs[v]), 64, 4)
+    if algo in ("msbfs", "msssp"):
+        srcs = msbfs_sources(g.n, lambda v: int(g.offs[v + 1]) - int(g.offs[v]), w["sources"], 4)
     threads = oracle.omp_threads()
     for _ in range(max(args.warmup - 1, 0)):
         cpu_run(w, g, csc, src, srcs, threads, budget_s=0.0, max_runs=1)

@@ -137,6 +137,7 @@ def _load():
         "grus_bfs_trace": ([vp, C.POINTER(LevelTrace), i32], i32),
         "grus_sssp_trace": ([vp, C.POINTER(LevelTrace), i32], i32),
         "grus_bfs_multi": ([vp, vp, i32, vp, C.POINTER(Stats), vp], i32),
+        "grus_sssp_multi": ([vp, vp, i32, vp, C.POINTER(Stats), vp], i32),
         "grus_batch_create": ([C.POINTER(vp), i32, C.POINTER(BatchConfig), PG], i32),
         "grus_batch_run": ([vp, C.POINTER(Query), i32, vp, i32, C.POINTER(Stats), vp], i32),
         "grus_batch_get_info": ([vp, C.POINTER(BatchConfig)], i32),
@@ -376,6 +377,19 @@ def bfs_multi(g: Graph, srcs, out=None, stream=None, stats: bool = False):
     _check(lib.grus_bfs_multi(g._handle(), _ptr(srcs), k, _ptr(out),
                               C.byref(st) if st is not None else None, _stream(stream)),
            "grus_bfs_multi")
+    return (out, st.as_dict()) if stats else out
+
+
+def sssp_multi(g: Graph, srcs, out=None, stream=None, stats: bool = False):
+    """Distances from up to 32 sources at once: a (k, n) uint32 array."""
+    srcs = np.ascontiguousarray(srcs, dtype=np.uint32)
+    k = int(srcs.size)
+    if out is None:
+        out = np.empty((k, g.n), np.uint32)
+    st = Stats() if stats else None
+    _check(lib.grus_sssp_multi(g._handle(), _ptr(srcs), k, _ptr(out),
+                               C.byref(st) if st is not None else None, _stream(stream)),
+           "grus_sssp_multi")
     return (out, st.as_dict()) if stats else out
 
 

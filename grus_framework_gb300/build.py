@@ -36,6 +36,7 @@ SOURCES = [
     "cc.cu",
     "pagerank.cu",
     "msbfs.cu",
+    "msssp.cu",
     "batch.cu",
     "serve.cu",
     "tune.cu",

@@ -166,7 +166,7 @@ struct RelaxVisitor {
     const uint32_t v = __ldg(g->cols + x);
     const uint32_t nd = du + __ldg(g->wts + x);
     if (nd >= __ldcg(dist + v)) return;
-    if (atomicMin(dist + v, nd) <= nd) return;
+    atomicMin(dist + v, nd);  // reduction; the bitmaps deduplicate the marks
     if (nd < T) {
       to_near(v);
     } else {

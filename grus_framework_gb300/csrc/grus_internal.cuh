@@ -40,7 +40,7 @@ struct Csr {
 };
 
 // Per-algorithm default workspaces cached on the graph handle.
-enum WsSlot { kWsBfs = 0, kWsSssp, kWsCc, kWsPr, kWsMsBfs, kWsCount = 8 };
+enum WsSlot { kWsBfs = 0, kWsSssp, kWsCc, kWsPr, kWsMsBfs, kWsMsSssp, kWsCount = 8 };
 
 }  // namespace grus
 
@@ -82,6 +82,9 @@ int launch_persistent(const void *fn, void **args, int block, int per_sm_req,
 // the depths from hsrc[i] (host array), 1 <= k <= 64.  With stats the call
 // waits for the launch and checks its error word.
 int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
+              grus_stats *stats, cudaStream_t s);
+// Multi-source SSSP (msssp.cu): as msbfs_run for distances, 1 <= k <= 32.
+int msssp_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
               grus_stats *stats, cudaStream_t s);
 
 }  // namespace grus

@@ -181,7 +181,10 @@ struct RelaxVisitor {
     const uint32_t v = __ldg(a->cols + x);
     const uint32_t nd = du + __ldg(a->wts + x);
     if (nd >= __ldcg(a->dist + v)) return;
-    if (atomicMin(a->dist + v, nd) <= nd) return;
+    // a reduction: the old value is not waited for.  If another thread
+    // lowered dist(v) further meanwhile, v is still marked below (the
+    // bitmaps deduplicate), costing at most one redundant expansion.
+    atomicMin(a->dist + v, nd);
     if (nd < T) {
       to_near(*a, v, inq_next, qnext, cnext, nx);
     } else {

@@ -172,6 +172,16 @@ GRUS_API int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth, grus_stats *
 GRUS_API int grus_bfs_multi(grus_graph *g, const uint32_t *srcs, int k, uint32_t *depths,
                    grus_stats *stats, void *stream);
 
+/* Multi-source SSSP: k <= 32 sources advance together in one persistent
+ * launch over one vertex-major distance matrix, sharing every adjacency
+ * read.  `srcs` (host or device) may repeat vertices; `dists` holds k*n
+ * uint32, source-major, bit-exact with k grus_sssp calls.  The reference
+ * answers one source per run of its SSSP sample (samples/sssp/sssp.cu:
+ * 123-170).  stats: levels, threshold advances (direction_switches),
+ * relaxations, and reach counts summed over the sources. */
+GRUS_API int grus_sssp_multi(grus_graph *g, const uint32_t *srcs, int k, uint32_t *dists,
+                    grus_stats *stats, void *stream);
+
 /* Per-level record of the last grus_bfs call made with stats: level i ends
  * end_ns after the kernel started; `vertices` were discovered into level i+1
  * with `edges` out-edges in total; `pull` is 1 for a bottom-up level. */
