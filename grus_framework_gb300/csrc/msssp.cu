@@ -15,11 +15,11 @@
 //   1. compacts the vertices with F[v] != 0 into work entries (v, begin, end,
 //      mask) of at most kPiece edges, clearing F[v] as it reads it (one
 //      atomic per CTA for the reservation);
-//   2. relaxes the entries: a warp takes one entry, its lanes are KS sources
-//      times 32/KS edges per step; a lane whose candidate beats the distance
-//      it read lowers it with a reduction (no round trip), and the lanes of
-//      one edge merge their bits into F'[v] (new distance < T) or Far[v] with
-//      one atomicOr each.
+//   2. relaxes the entries: a warp takes one entry and deals its lanes the
+//      (edge, active source) pairs of it, so work follows the pairs that are
+//      live rather than edges x 32; a lane whose candidate beats the distance
+//      it read lowers it with a reduction (no round trip) and sets the pair's
+//      bit in F'[v] (new distance < T) or Far[v].
 // When a level finds no entry, T advances by Delta (or jumps to the bucket of
 // the smallest far distance) and Far is scanned: pairs below the old T were
 // already expanded and are dropped, pairs below the new T move to F.
@@ -113,58 +113,56 @@ __device__ __forceinline__ void build_entries(const Args &a, uint32_t *F, Slot *
   }
 }
 
-// Step 2: one entry per warp.  Lane = g * KS + s: source s, edge group g.
+// Step 2: one entry per warp.  Only the p sources whose bit is set in the
+// entry's mask do work: the lanes are dealt (edge, active source) pairs,
+// lane = j * p + i takes the i-th active source of edge j, so a warp step
+// covers floor(32 / p) edges and every lane of it relaxes a live pair (a
+// lane per source would leave 32 - p lanes idle on every edge).
 template <int KS>
 __device__ __forceinline__ unsigned long long relax_entry(const Args &a, const uint4 ent,
                                                           uint32_t *Fn, uint32_t T) {
-  constexpr int G = 32 / KS;
   const uint32_t lane = lane_id();
-  const uint32_t s = lane % KS, g = lane / KS;
   const uint32_t u = ent.x, b = ent.y, e = ent.z, mask = ent.w;
-  const bool act = (mask >> s) & 1u;
-  const uint32_t du = act ? __ldcg(a.D + (size_t)u * KS + s) : 0u;
-  const uint32_t gshift = g * KS;
-  const uint32_t gmask = KS == 32 ? 0xffffffffu : ((1u << KS) - 1u);
+  const uint32_t p = __popc(mask);
+  // distance of u from source `lane`, handed to the lanes by shuffle
+  const uint32_t du_all = (lane < (uint32_t)KS && ((mask >> lane) & 1u))
+                              ? __ldcg(a.D + (size_t)u * KS + lane) : 0u;
+  const uint32_t eps = 32u / p;           // edges per warp step
+  const uint32_t j = lane / p, i = lane - j * p;
+  const bool live = j < eps;
+  const uint32_t s = __fns(mask, 0, (int)i + 1);  // i-th set bit of the mask
+  const uint32_t du = __shfl_sync(0xffffffffu, du_all, live ? s : 0u);
+  const uint32_t bit = 1u << (s & 31u);
   for (uint32_t x0 = b; x0 < e; x0 += 32) {
     const uint32_t xi = x0 + lane;
     const uint32_t c = xi < e ? __ldg(a.cols + xi) : 0u;
     const uint32_t w = xi < e ? __ldg(a.wts + xi) : 0u;
     const uint32_t ne = min(32u, e - x0);
-    for (uint32_t j0 = 0; j0 < ne; j0 += 4 * G) {
+    for (uint32_t j0 = 0; j0 < ne; j0 += 4 * eps) {
       uint32_t v[4], nd[4], cur[4];
       bool ok[4];
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
-        const uint32_t j = j0 + r * G + g;
-        ok[r] = j < ne;
-        v[r] = __shfl_sync(0xffffffffu, c, j & 31u);
-        nd[r] = du + __shfl_sync(0xffffffffu, w, j & 31u);
+        const uint32_t jj = j0 + r * eps + j;
+        ok[r] = live && jj < ne;
+        v[r] = __shfl_sync(0xffffffffu, c, jj & 31u);
+        nd[r] = du + __shfl_sync(0xffffffffu, w, jj & 31u);
       }
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
-        cur[r] = (ok[r] && act) ? __ldcg(a.D + (size_t)v[r] * KS + s) : 0u;
+      for (int r = 0; r < 4; ++r) cur[r] = ok[r] ? __ldcg(a.D + (size_t)v[r] * KS + s) : 0u;
       // The lowering is a reduction whose old value is not waited for: a pair
       // that another lane lowered further in the meantime is marked again,
       // which costs at most one redundant expansion and never a missed one.
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
-        const bool imp = ok[r] && act && nd[r] < cur[r];
-        if (imp) atomicMin(a.D + (size_t)v[r] * KS + s, nd[r]);
-      }
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const bool imp = ok[r] && act && nd[r] < cur[r];
-        const uint32_t nb = __ballot_sync(0xffffffffu, imp && nd[r] < T);
-        const uint32_t fb = __ballot_sync(0xffffffffu, imp && nd[r] >= T);
-        if (s == 0 && ok[r]) {
-          const uint32_t mn = (nb >> gshift) & gmask, mf = (fb >> gshift) & gmask;
-          if (mn) atomicOr(Fn + v[r], mn);
-          if (mf) atomicOr(a.far + v[r], mf);
+        if (ok[r] && nd[r] < cur[r]) {
+          atomicMin(a.D + (size_t)v[r] * KS + s, nd[r]);
+          atomicOr((nd[r] < T ? Fn : a.far) + v[r], bit);
         }
       }
     }
   }
-  return s == 0 && g == 0 ? (unsigned long long)__popc(mask) * (e - b) : 0ull;
+  return lane == 0 ? (unsigned long long)p * (e - b) : 0ull;
 }
 
 template <int KS>
