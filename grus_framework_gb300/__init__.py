@@ -78,7 +78,8 @@ class Query(C.Structure):
 
 class BatchConfig(C.Structure):
     _fields_ = [("cluster_size", C.c_uint32), ("workers", C.c_uint32),
-                ("huge_degree", C.c_uint32), ("sssp_delta", C.c_uint32)]
+                ("huge_degree", C.c_uint32), ("sssp_delta", C.c_uint32),
+                ("group_sources", C.c_uint32)]
 
 
 class ServerConfig(C.Structure):
@@ -452,9 +453,10 @@ class Batch:
     """Many BFS / SSSP queries over several resident graphs in one launch
     (cluster workers, include/grus.h grus_batch_*)."""
 
-    def __init__(self, graphs, cluster_size=0, workers=0, huge_degree=0, sssp_delta=0):
+    def __init__(self, graphs, cluster_size=0, workers=0, huge_degree=0, sssp_delta=0,
+                 group_sources=0):
         self.graphs = list(graphs)
-        cfg = BatchConfig(cluster_size, workers, huge_degree, sssp_delta)
+        cfg = BatchConfig(cluster_size, workers, huge_degree, sssp_delta, group_sources)
         h = C.c_void_p()
         _check(lib.grus_batch_create(_graph_array(self.graphs), len(self.graphs), C.byref(cfg),
                                      C.byref(h)), "grus_batch_create")

@@ -12,6 +12,10 @@
 //          warp / gather mappings, hub chunks), visited bitmap claims.
 //   SSSP : the near/far label-correcting scheme of sssp.cu (atomicMin,
 //          Delta buckets), scoped to the cluster.
+//   SSSP group : up to 32 SSSP queries on one graph as ONE multi-source
+//          traversal (msssp_core.cuh) scoped to the cluster, sharing every
+//          adjacency read; the host packs queries on the same graph into
+//          such groups.
 // Results are bit-exact against single-query runs (BFS depths and SSSP
 // distances are schedule-independent).  The same kernel, launched with one
 // worker on a stream, is the unit of work of the query server (serve.cu).
@@ -26,6 +30,7 @@
 #include "batch.cuh"
 #include "expand.cuh"
 #include "grus_internal.cuh"
+#include "msssp_core.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -53,6 +58,7 @@ struct WorkerCtl {
   unsigned long long pad[12];
 };
 static_assert(sizeof(WorkerCtl) == 256, "control block layout");
+static_assert(sizeof(Slot) == sizeof(ms::Slot), "multi-source slots reuse the worker slots");
 
 struct Args {
   const GraphDesc *graphs;
@@ -69,6 +75,13 @@ struct Args {
   uint32_t cap, chunk_cap;
   uint32_t huge, delta;
   uint32_t *err;
+  // multi-source groups
+  const uint32_t *msrc;
+  const unsigned long long *moff;
+  uint32_t *ms_d, *ms_masks;
+  uint4 *ms_ent;
+  uint64_t ms_n;
+  uint32_t ms_ks, ms_ent_cap;
 };
 
 struct Ctx {
@@ -277,6 +290,51 @@ __device__ void run_sssp(const Args &a, const Ctx &c, cg::cluster_group &cl, con
   cl.sync();
 }
 
+// ---- SSSP group -----------------------------------------------------------
+struct ClusterSync {
+  cg::cluster_group *cl;
+  __device__ __forceinline__ bool operator()() const {
+    cl->sync();
+    return true;
+  }
+};
+
+struct GroupOut {
+  uint32_t *out;
+  const unsigned long long *moff;
+  __device__ __forceinline__ uint32_t *operator()(uint32_t s) const { return out + moff[s]; }
+};
+
+__device__ void run_msssp(const Args &a, const Ctx &c, cg::cluster_group &cl, const GraphDesc *g,
+                          const Task &task, uint32_t worker, WorkerCtl *ctl) {
+  ms::View v;
+  v.offs = g->offs;
+  v.cols = g->cols;
+  v.wts = g->wts;
+  v.n = g->n;
+  v.k = task.pad;
+  v.srcs = a.msrc + task.src;
+  v.D = a.ms_d + (uint64_t)worker * a.ms_n * a.ms_ks;
+  uint32_t *masks = a.ms_masks + (uint64_t)worker * 3 * a.ms_n;
+  v.F[0] = masks;
+  v.F[1] = masks + a.ms_n;
+  v.far = masks + 2 * a.ms_n;
+  v.ent = a.ms_ent + (uint64_t)worker * a.ms_ent_cap;
+  v.ent_cap = a.ms_ent_cap;
+  v.slots = (ms::Slot *)ctl->slots;
+  v.minfar = ctl->far.minfar;
+  v.err = &ctl->err;
+  v.delta = a.delta;
+  ClusterSync sync{&cl};
+  GroupOut out{a.out, a.moff + task.src};
+  ms::Result r;
+  if (v.k <= 8) ms::run<8, kBatchBlock>(v, c.ctid, c.cthreads, sync, out, r);
+  else if (v.k <= 16) ms::run<16, kBatchBlock>(v, c.ctid, c.cthreads, sync, out, r);
+  else ms::run<32, kBatchBlock>(v, c.ctid, c.cthreads, sync, out, r);
+  if (c.ctid == 0) ctl->levels = r.levels;
+  cl.sync();
+}
+
 __global__ void __launch_bounds__(kBatchBlock, 4) batch_kernel(Args a) {
   cg::cluster_group cl = cg::this_cluster();
   __shared__ uint32_t s_task;
@@ -302,7 +360,12 @@ __global__ void __launch_bounds__(kBatchBlock, 4) batch_kernel(Args a) {
     const Task task = a.tasks[t];
     const GraphDesc *g = a.graphs + task.graph;
     uint32_t *out = a.out + task.out_off;
-    if (task.algo == kAlgoSssp && g->wts)
+    if (task.algo == kAlgoSsspMulti) {
+      if (g->wts && a.ms_d && task.pad >= 1 && task.pad <= a.ms_ks)
+        run_msssp(a, c, cl, g, task, worker, ctl);
+      else if (c.ctid == 0)
+        atomicOr(&ctl->err, kErrOverflow);  // no group state: the host sized it wrong
+    } else if (task.algo == kAlgoSssp && g->wts)
       run_sssp(a, c, cl, g, task.src, out, bm, lists, chunks, ctl);
     else
       run_bfs(a, c, cl, g, task.src, out, bm, lists, chunks, ctl);
@@ -350,7 +413,40 @@ int batch_occupancy(int cluster, int *workers) {
   return GRUS_OK;
 }
 
+void BatchState::release_multi() {
+  cudaFree(ms_d);
+  cudaFree(ms_masks);
+  cudaFree(ms_ent);
+  ms_d = ms_masks = nullptr;
+  ms_ent = nullptr;
+  ms_n = 0;
+  ms_ks = ms_ent_cap = 0;
+  ms_workers = 0;
+}
+
+int BatchState::reserve_multi(int nworkers, uint64_t max_n, uint64_t max_m, uint32_t ks) {
+  const uint64_t n1 = std::max<uint64_t>(max_n, 1);
+  const uint32_t ecap = (uint32_t)std::min<uint64_t>(n1 + max_m / ms::kPiece + 1024, 0xFFFFFFF0ull);
+  if (nworkers <= ms_workers && n1 <= ms_n && ks <= ms_ks && ecap <= ms_ent_cap) return GRUS_OK;
+  release_multi();
+  cudaError_t e = cudaMalloc(&ms_d, (uint64_t)nworkers * n1 * ks * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&ms_masks, (uint64_t)nworkers * 3 * n1 * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&ms_ent, (uint64_t)nworkers * ecap * sizeof(uint4));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    release_multi();
+    set_last_error(std::string("batch multi-source state: ") + cudaGetErrorString(e));
+    return status_from_cuda(e);
+  }
+  ms_n = n1;
+  ms_ks = ks;
+  ms_ent_cap = ecap;
+  ms_workers = nworkers;
+  return GRUS_OK;
+}
+
 void BatchState::release() {
+  release_multi();
   cudaFree(bitmaps);
   cudaFree(lists);
   cudaFree(chunks);
@@ -398,7 +494,8 @@ size_t BatchState::bytes_per_worker(uint64_t max_n, uint64_t max_m, uint32_t hug
 
 int batch_launch(BatchState &st, int worker0, int nworkers, int cluster, const GraphDesc *graphs,
                  const Task *tasks, uint32_t ntasks, uint32_t *out, uint32_t huge, uint32_t delta,
-                 uint32_t *counter, cudaStream_t s) {
+                 uint32_t *counter, cudaStream_t s, const uint32_t *msrc,
+                 const unsigned long long *moff) {
   Args a;
   std::memset(&a, 0, sizeof(a));
   a.graphs = graphs;
@@ -416,6 +513,16 @@ int batch_launch(BatchState &st, int worker0, int nworkers, int cluster, const G
   a.huge = huge;
   a.delta = std::max(delta, 1u);
   a.err = st.err;
+  a.msrc = msrc;
+  a.moff = moff;
+  if (msrc && st.ms_d && worker0 + nworkers <= st.ms_workers) {
+    a.ms_d = st.ms_d + (uint64_t)worker0 * st.ms_n * st.ms_ks;
+    a.ms_masks = st.ms_masks + (uint64_t)worker0 * 3 * st.ms_n;
+    a.ms_ent = st.ms_ent + (uint64_t)worker0 * st.ms_ent_cap;
+    a.ms_n = st.ms_n;
+    a.ms_ks = st.ms_ks;
+    a.ms_ent_cap = st.ms_ent_cap;
+  }
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeClusterDimension;
   attr.val.clusterDim.x = cluster;
@@ -454,13 +561,19 @@ struct grus_batch {
   grus::GraphDesc *d_graphs = nullptr;
   grus::Task *d_tasks = nullptr, *h_tasks = nullptr;  // pinned staging
   uint32_t task_cap = 0;
+  // members of multi-source groups: sources and output offsets (pinned staging)
+  uint32_t *d_msrc = nullptr, *h_msrc = nullptr;
+  unsigned long long *d_moff = nullptr, *h_moff = nullptr;
+  uint32_t member_cap = 0;
+  uint32_t group = 1;                  // SSSP queries per multi-source group
+  uint32_t ntasks = 0, nmembers = 0;   // of the staged plan
   grus::BatchState state;
   int cluster = 16, workers = 0;
   uint32_t huge = 1024, delta = 96;
   uint64_t max_n = 0, max_m = 0, total_out = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  uint32_t graph_ntasks = 0;
+  uint32_t graph_ntasks = 0, graph_nmembers = 0;
   uint32_t *graph_out = nullptr;
   cudaStream_t graph_stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -492,6 +605,12 @@ int grus_batch_create(grus_graph *const *graphs, int ngraphs, const grus_batch_c
     if (cfg->huge_degree) b->huge = cfg->huge_degree;
     if (cfg->sssp_delta) b->delta = cfg->sssp_delta;
     if (cfg->workers) b->workers = (int)cfg->workers;
+    if (cfg->group_sources) b->group = cfg->group_sources;
+  }
+  if (b->group < 1 || b->group > (uint32_t)kMaxGroup) {
+    delete b;
+    set_last_error("group_sources must be 1..32");
+    return GRUS_EINVAL;
   }
   if (b->cluster < 1 || b->cluster > 16) {
     delete b;
@@ -527,14 +646,18 @@ int grus_batch_create(grus_graph *const *graphs, int ngraphs, const grus_batch_c
   return GRUS_OK;
 }
 
-static int ensure_tasks(grus_batch *b, uint32_t n) {
-  if (n <= b->task_cap) return GRUS_OK;
+static void drop_graph(grus_batch *b) {
   if (b->exec) {  // a captured graph points at the old buffers
     cudaGraphExecDestroy(b->exec);
     cudaGraphDestroy(b->graph);
     b->exec = nullptr;
     b->graph = nullptr;
   }
+}
+
+static int ensure_tasks(grus_batch *b, uint32_t n) {
+  if (n <= b->task_cap) return GRUS_OK;
+  drop_graph(b);
   cudaFree(b->d_tasks);
   cudaFreeHost(b->h_tasks);
   b->d_tasks = nullptr;
@@ -546,22 +669,110 @@ static int ensure_tasks(grus_batch *b, uint32_t n) {
   return GRUS_OK;
 }
 
-// Work items in descending graph size first, so large queries start early.
-static void stage_tasks(grus_batch *b, const grus_query *q, int nq) {
+static int ensure_members(grus_batch *b, uint32_t n) {
+  if (n <= b->member_cap) return GRUS_OK;
+  drop_graph(b);
+  cudaFree(b->d_msrc);
+  cudaFree(b->d_moff);
+  cudaFreeHost(b->h_msrc);
+  cudaFreeHost(b->h_moff);
+  b->d_msrc = b->h_msrc = nullptr;
+  b->d_moff = b->h_moff = nullptr;
+  b->member_cap = 0;
+  GRUS_CUDA_TRY(cudaMalloc(&b->d_msrc, n * 4));
+  GRUS_CUDA_TRY(cudaMalloc(&b->d_moff, n * 8));
+  GRUS_CUDA_TRY(cudaMallocHost(&b->h_msrc, n * 4));
+  GRUS_CUDA_TRY(cudaMallocHost(&b->h_moff, n * 8));
+  b->member_cap = n;
+  return GRUS_OK;
+}
+
+// Cost model of one task on one worker, in edge-equivalents: a traversal
+// reads the edges and scans the vertex arrays; each extra source of a
+// multi-source task adds about a third of a single traversal (measured on
+// RMAT graphs: 8 sources cost 3.25 single queries on a 16-CTA worker).
+static double task_cost(const grus_graph *g, int k) {
+  return ((double)g->m + 16.0 * (double)g->n) * (1.0 + 0.32 * (k - 1));
+}
+
+// Plans the run: SSSP queries on the same graph are packed into
+// multi-source tasks of up to `group` queries, but a pack never costs more
+// than the larger of the most expensive single query and the batch's even
+// share per worker, so packing lowers the total work without lengthening the
+// critical path (the largest graphs keep one query per worker).  Tasks are
+// ordered by descending graph size so large work starts first.
+static int stage_tasks(grus_batch *b, const grus_query *q, int nq) {
   std::vector<int> order(nq);
   for (int i = 0; i < nq; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-    return b->graphs[q[x].graph]->m > b->graphs[q[y].graph]->m;
+    const uint64_t mx = b->graphs[q[x].graph]->m, my = b->graphs[q[y].graph]->m;
+    if (mx != my) return mx > my;
+    if (q[x].graph != q[y].graph) return q[x].graph < q[y].graph;
+    return q[x].algo < q[y].algo;
   });
+  struct Plan {
+    Task t;
+    int first, k;  // members (multi-source) or -1
+  };
+  std::vector<Plan> plan;
+  std::vector<int> members;
+  uint32_t max_k = 0;
+  double total = 0.0, top = 0.0;
   for (int i = 0; i < nq; ++i) {
-    const grus_query &s = q[order[i]];
-    Task &t = b->h_tasks[i];
-    t.graph = s.graph;
-    t.algo = s.algo;
-    t.src = s.src;
-    t.pad = 0;
-    t.out_off = s.out_offset;
+    const double c = task_cost(b->graphs[q[i].graph], 1);
+    total += c;
+    top = std::max(top, c);
   }
+  const double target = std::max(top, total / std::max(b->workers, 1));
+  for (int i = 0; i < nq;) {
+    const grus_query &s0 = q[order[i]];
+    const grus_graph *g0 = b->graphs[s0.graph];
+    int j = i + 1;
+    if (b->group > 1 && s0.algo == GRUS_ALGO_SSSP)
+      while (j < nq && j - i < (int)b->group && q[order[j]].graph == s0.graph &&
+             q[order[j]].algo == GRUS_ALGO_SSSP && task_cost(g0, j - i + 1) <= target)
+        ++j;
+    Plan p;
+    p.t.graph = s0.graph;
+    p.t.pad = 0;
+    p.t.out_off = s0.out_offset;
+    if (j - i >= 2) {
+      p.t.algo = kAlgoSsspMulti;
+      p.first = (int)members.size();
+      p.k = j - i;
+      p.t.src = (uint32_t)p.first;
+      p.t.pad = (uint32_t)p.k;
+      for (int x = i; x < j; ++x) members.push_back(order[x]);
+      max_k = std::max<uint32_t>(max_k, (uint32_t)p.k);
+    } else {
+      j = i + 1;
+      p.t.algo = s0.algo;
+      p.t.src = s0.src;
+      p.first = -1;
+      p.k = 0;
+    }
+    plan.push_back(p);
+    i = j;
+  }
+  int rc = ensure_tasks(b, (uint32_t)plan.size());
+  if (rc) return rc;
+  if (!members.empty()) {
+    rc = ensure_members(b, (uint32_t)members.size());
+    if (rc) return rc;
+    const uint32_t ks = max_k <= 8 ? 8u : (max_k <= 16 ? 16u : 32u);
+    const uint32_t *before = b->state.ms_d;
+    rc = b->state.reserve_multi(b->workers, b->max_n, b->max_m, ks);
+    if (rc) return rc;
+    if (b->state.ms_d != before) drop_graph(b);  // a captured launch holds the old state
+  }
+  for (size_t i = 0; i < plan.size(); ++i) b->h_tasks[i] = plan[i].t;
+  for (size_t i = 0; i < members.size(); ++i) {
+    b->h_msrc[i] = q[members[i]].src;
+    b->h_moff[i] = q[members[i]].out_offset;
+  }
+  b->ntasks = (uint32_t)plan.size();
+  b->nmembers = (uint32_t)members.size();
+  return GRUS_OK;
 }
 
 int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *out,
@@ -582,46 +793,54 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
     return GRUS_EINVAL;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  // the pinned staging buffer is read by the previous run's copy: wait for it
+  // the pinned staging buffers are read by the previous run's copies: wait
   if (b->in_flight) GRUS_CUDA_TRY(cudaEventSynchronize(b->done));
-  int rc = ensure_tasks(b, (uint32_t)nq);
+  int rc = stage_tasks(b, queries, nq);
   if (rc) return rc;
-  stage_tasks(b, queries, nq);
+  const uint32_t nt = b->ntasks, nm = b->nmembers;
+  const uint32_t *msrc = nm ? b->d_msrc : nullptr;
+  const unsigned long long *moff = nm ? b->d_moff : nullptr;
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(b->ev0, s));
   if (use_graph) {
     // one captured graph per (task count, output buffer): H2D copy of the
     // staged tasks, counter reset, batch kernel
-    if (b->exec && (b->graph_ntasks != (uint32_t)nq || b->graph_out != out || b->graph_stream != s)) {
-      cudaGraphExecDestroy(b->exec);
-      cudaGraphDestroy(b->graph);
-      b->exec = nullptr;
-      b->graph = nullptr;
-    }
+    if (b->exec && (b->graph_ntasks != nt || b->graph_nmembers != nm || b->graph_out != out ||
+                    b->graph_stream != s))
+      drop_graph(b);
     if (!b->exec) {
       cudaStream_t cap_s = nullptr;
       GRUS_CUDA_TRY(cudaStreamCreateWithFlags(&cap_s, cudaStreamNonBlocking));
       cudaError_t e = cudaStreamBeginCapture(cap_s, cudaStreamCaptureModeThreadLocal);
       if (e == cudaSuccess) {
-        cudaMemcpyAsync(b->d_tasks, b->h_tasks, nq * sizeof(Task), cudaMemcpyHostToDevice, cap_s);
+        cudaMemcpyAsync(b->d_tasks, b->h_tasks, nt * sizeof(Task), cudaMemcpyHostToDevice, cap_s);
+        if (nm) {
+          cudaMemcpyAsync(b->d_msrc, b->h_msrc, nm * 4, cudaMemcpyHostToDevice, cap_s);
+          cudaMemcpyAsync(b->d_moff, b->h_moff, nm * 8, cudaMemcpyHostToDevice, cap_s);
+        }
         cudaMemsetAsync(b->state.counter, 0, 4, cap_s);
-        rc = batch_launch(b->state, 0, b->workers, b->cluster, b->d_graphs, b->d_tasks, nq, out,
-                          b->huge, b->delta, b->state.counter, cap_s);
+        rc = batch_launch(b->state, 0, b->workers, b->cluster, b->d_graphs, b->d_tasks, nt, out,
+                          b->huge, b->delta, b->state.counter, cap_s, msrc, moff);
         e = cudaStreamEndCapture(cap_s, &b->graph);
       }
       cudaStreamDestroy(cap_s);
       if (rc) return rc;
       GRUS_CUDA_TRY(e);
       GRUS_CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
-      b->graph_ntasks = (uint32_t)nq;
+      b->graph_ntasks = nt;
+      b->graph_nmembers = nm;
       b->graph_out = out;
       b->graph_stream = s;
     }
     GRUS_CUDA_TRY(cudaGraphLaunch(b->exec, s));
   } else {
-    GRUS_CUDA_TRY(cudaMemcpyAsync(b->d_tasks, b->h_tasks, nq * sizeof(Task), cudaMemcpyHostToDevice, s));
+    GRUS_CUDA_TRY(cudaMemcpyAsync(b->d_tasks, b->h_tasks, nt * sizeof(Task), cudaMemcpyHostToDevice, s));
+    if (nm) {
+      GRUS_CUDA_TRY(cudaMemcpyAsync(b->d_msrc, b->h_msrc, nm * 4, cudaMemcpyHostToDevice, s));
+      GRUS_CUDA_TRY(cudaMemcpyAsync(b->d_moff, b->h_moff, nm * 8, cudaMemcpyHostToDevice, s));
+    }
     GRUS_CUDA_TRY(cudaMemsetAsync(b->state.counter, 0, 4, s));
-    rc = batch_launch(b->state, 0, b->workers, b->cluster, b->d_graphs, b->d_tasks, nq, out, b->huge,
-                      b->delta, b->state.counter, s);
+    rc = batch_launch(b->state, 0, b->workers, b->cluster, b->d_graphs, b->d_tasks, nt, out, b->huge,
+                      b->delta, b->state.counter, s, msrc, moff);
     if (rc) return rc;
   }
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(b->ev1, s));
@@ -650,6 +869,7 @@ int grus_batch_get_info(const grus_batch *b, grus_batch_config *info) {
   info->workers = (uint32_t)b->workers;
   info->huge_degree = b->huge;
   info->sssp_delta = b->delta;
+  info->group_sources = b->group;
   return GRUS_OK;
 }
 
@@ -662,6 +882,10 @@ int grus_batch_free(grus_batch *b) {
   cudaFree(b->d_graphs);
   cudaFree(b->d_tasks);
   if (b->h_tasks) cudaFreeHost(b->h_tasks);
+  cudaFree(b->d_msrc);
+  cudaFree(b->d_moff);
+  if (b->h_msrc) cudaFreeHost(b->h_msrc);
+  if (b->h_moff) cudaFreeHost(b->h_moff);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   if (b->done) cudaEventDestroy(b->done);

@@ -1,57 +1,27 @@
-// msssp.cu -- multi-source SSSP: up to 32 sources in ONE persistent launch.
+// msssp.cu -- multi-source SSSP: up to 32 sources in ONE persistent launch
+// over the whole GPU (the level loop is msssp_core.cuh; levels are separated
+// by the bounded grid barrier).
 //
 // The reference runs one SSSP per process invocation
 // (samples/sssp/sssp.cu:123-170); 32 queries on one graph cost 32 launches of
 // its level loop, each re-reading the adjacency lists.  Here the sources
-// advance together and share every adjacency read:
-//   D[v][s]   distance of v from source s, vertex-major (KS u32 per vertex, one
-//             32/64/128-byte row), so the KS distances of a vertex are one
-//             coalesced access;
-//   F[v]      bit s set if (v, s) improved below the threshold T and must be
-//             expanded (near frontier, two arrays used in turn);
-//   Far[v]    bit s set if (v, s) improved to a distance >= T (far pile).
-// It is the near/far label-correcting scheme of sssp.cu run per (v, s) pair
-// with one shared threshold T.  A level
-//   1. compacts the vertices with F[v] != 0 into work entries (v, begin, end,
-//      mask) of at most kPiece edges, clearing F[v] as it reads it (one
-//      atomic per CTA for the reservation);
-//   2. relaxes the entries: a warp takes one entry and deals its lanes the
-//      (edge, active source) pairs of it, so work follows the pairs that are
-//      live rather than edges x 32; a lane whose candidate beats the distance
-//      it read lowers it with a reduction (no round trip) and sets the pair's
-//      bit in F'[v] (new distance < T) or Far[v].
-// When a level finds no entry, T advances by Delta (or jumps to the bucket of
-// the smallest far distance) and Far is scanned: pairs below the old T were
-// already expanded and are dropped, pairs below the new T move to F.
-// Every wait is a bounded grid barrier.  Each (v, s) pair reaches Dijkstra's
-// distance whatever the schedule, so the outputs are bit-exact against
-// single-source runs.
+// advance together and share every adjacency read, and the outputs are
+// bit-exact against single-source runs.
 #include <algorithm>
 #include <cstring>
 
 #include "device_util.cuh"
 #include "grus_internal.cuh"
+#include "msssp_core.cuh"
 
 namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr uint32_t kPiece = 128;      // edges per work entry
 constexpr uint32_t kDefDelta = 96;
 constexpr int kMaxSources = 32;
-
-struct Slot {
-  uint32_t nent;          // work entries of the level
-  uint32_t moved;         // pairs moved from far to near by a split
-  uint32_t remaining;     // vertices still holding far pairs after a split
-  uint32_t pad0;
-  unsigned long long visits;
-  uint32_t pad[10];
-};
-
-struct FarCtl {
-  uint32_t minfar[2];
-};
+using ms::kPiece;
+using ms::Slot;
 
 struct Summary {
   uint32_t levels, splits, pad0, pad1;
@@ -59,237 +29,43 @@ struct Summary {
 };
 
 struct Args {
-  const uint32_t *__restrict__ offs;
-  const uint32_t *__restrict__ cols;
-  const uint32_t *__restrict__ wts;
-  uint32_t n, k;
-  const uint32_t *srcs;
+  ms::View v;
   uint32_t *out[kMaxSources];
-  uint32_t *D;
-  uint32_t *F[2];
-  uint32_t *far;
-  uint4 *ent;
-  uint32_t ent_cap;
-  Slot *slots;
-  FarCtl *farctl;
   GridBarrier *bar;
-  uint32_t *err;
   Summary *summary;
-  uint32_t delta;
   uint64_t timeout_ns;
 };
 
-// Step 1: vertices with a non-empty near mask become work entries.
-__device__ __forceinline__ void build_entries(const Args &a, uint32_t *F, Slot *sl, uint32_t gtid,
-                                              uint32_t nthreads) {
-  const uint32_t rounds = (a.n + nthreads - 1) / nthreads;
-  for (uint32_t r = 0; r < rounds; ++r) {
-    const uint32_t v = r * nthreads + gtid;
-    uint32_t m = 0, b = 0, e = 0, nch = 0;
-    if (v < a.n) {
-      m = __ldcg(F + v);
-      if (m) {
-        F[v] = 0u;
-        b = __ldg(a.offs + v);
-        e = __ldg(a.offs + v + 1);
-        nch = (e - b + kPiece - 1) / kPiece;
-      }
-    }
-    uint32_t total = 0;
-    const uint32_t off = block_exclusive_scan<kBlock>(nch, &total);
-    __shared__ uint32_t s_base;
-    if (threadIdx.x == 0) s_base = total ? atomicAdd(&sl->nent, total) : 0u;
-    __syncthreads();
-    const uint32_t base = s_base + off;
-    if (nch) {
-      if (base + nch > a.ent_cap) {
-        atomicOr(a.err, kErrOverflow);
-      } else {
-        for (uint32_t c = 0; c < nch; ++c)
-          a.ent[base + c] = make_uint4(v, b + c * kPiece, min(e, b + (c + 1) * kPiece), m);
-      }
-    }
-    __syncthreads();
-  }
-}
+struct GridSync {
+  GridBarrier *bar;
+  uint32_t *err;
+  uint64_t timeout_ns;
+  __device__ __forceinline__ bool operator()() const { return grid_sync(bar, err, timeout_ns); }
+};
 
-// Step 2: one entry per warp.  Only the p sources whose bit is set in the
-// entry's mask do work: the lanes are dealt (edge, active source) pairs,
-// lane = j * p + i takes the i-th active source of edge j, so a warp step
-// covers floor(32 / p) edges and every lane of it relaxes a live pair (a
-// lane per source would leave 32 - p lanes idle on every edge).
-template <int KS>
-__device__ __forceinline__ unsigned long long relax_entry(const Args &a, const uint4 ent,
-                                                          uint32_t *Fn, uint32_t T) {
-  const uint32_t lane = lane_id();
-  const uint32_t u = ent.x, b = ent.y, e = ent.z, mask = ent.w;
-  const uint32_t p = __popc(mask);
-  // distance of u from source `lane`, handed to the lanes by shuffle
-  const uint32_t du_all = (lane < (uint32_t)KS && ((mask >> lane) & 1u))
-                              ? __ldcg(a.D + (size_t)u * KS + lane) : 0u;
-  const uint32_t eps = 32u / p;           // edges per warp step
-  const uint32_t j = lane / p, i = lane - j * p;
-  const bool live = j < eps;
-  const uint32_t s = __fns(mask, 0, (int)i + 1);  // i-th set bit of the mask
-  const uint32_t du = __shfl_sync(0xffffffffu, du_all, live ? s : 0u);
-  const uint32_t bit = 1u << (s & 31u);
-  for (uint32_t x0 = b; x0 < e; x0 += 32) {
-    const uint32_t xi = x0 + lane;
-    const uint32_t c = xi < e ? __ldg(a.cols + xi) : 0u;
-    const uint32_t w = xi < e ? __ldg(a.wts + xi) : 0u;
-    const uint32_t ne = min(32u, e - x0);
-    for (uint32_t j0 = 0; j0 < ne; j0 += 4 * eps) {
-      uint32_t v[4], nd[4], cur[4];
-      bool ok[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const uint32_t jj = j0 + r * eps + j;
-        ok[r] = live && jj < ne;
-        v[r] = __shfl_sync(0xffffffffu, c, jj & 31u);
-        nd[r] = du + __shfl_sync(0xffffffffu, w, jj & 31u);
-      }
-#pragma unroll
-      for (int r = 0; r < 4; ++r) cur[r] = ok[r] ? __ldcg(a.D + (size_t)v[r] * KS + s) : 0u;
-      // The lowering is a reduction whose old value is not waited for: a pair
-      // that another lane lowered further in the meantime is marked again,
-      // which costs at most one redundant expansion and never a missed one.
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        if (ok[r] && nd[r] < cur[r]) {
-          atomicMin(a.D + (size_t)v[r] * KS + s, nd[r]);
-          atomicOr((nd[r] < T ? Fn : a.far) + v[r], bit);
-        }
-      }
-    }
-  }
-  return lane == 0 ? (unsigned long long)p * (e - b) : 0ull;
-}
+struct OutTable {
+  uint32_t *const *out;
+  __device__ __forceinline__ uint32_t *operator()(uint32_t s) const { return out[s]; }
+};
 
 template <int KS>
 __global__ void __launch_bounds__(kBlock) msssp_persistent(Args a) {
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
-  const uint32_t gwarp = gtid >> 5, nwarps = nthreads >> 5;
-  // prologue
-  const size_t dn = (size_t)a.n * KS;
-  for (size_t i = gtid; i < dn; i += nthreads) a.D[i] = kInfinit;
-  for (uint32_t i = gtid; i < a.n; i += nthreads) {
-    a.F[0][i] = 0u;
-    a.F[1][i] = 0u;
-    a.far[i] = 0u;
-  }
-  if (gtid < 4 * sizeof(Slot) / 4) ((uint32_t *)a.slots)[gtid] = 0u;
-  if (gtid < sizeof(FarCtl) / 4) ((uint32_t *)a.farctl)[gtid] = 0xFFFFFFFFu;
-  if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-  if (gtid < a.k) {
-    const uint32_t src = a.srcs[gtid];
-    a.D[(size_t)src * KS + gtid] = 0u;
-    atomicOr(a.F[0] + src, 1u << gtid);
-  }
-  if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-
-  uint32_t L = 0, T = a.delta, splits = 0, sel = 0;
-  unsigned long long visits = 0;
-  while (true) {
-    Slot *sl = a.slots + (L & 3u);
-    // reset the slot used two levels ahead
-    if (gtid < sizeof(Slot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[gtid] = 0u;
-    build_entries(a, a.F[sel], sl, gtid, nthreads);
-    if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-    const uint32_t nent = min(__ldcg(&sl->nent), a.ent_cap);
-    if (nent == 0) {
-      // near frontier empty: advance T and split the far masks into F[sel]
-      const uint32_t Told = T;
-      uint32_t Tnew = T + a.delta;
-      // minfar[j & 1] holds the smallest distance left in the far masks by
-      // split j - 1; split j reduces into the other word and resets this one
-      // once every CTA has read it (after the next barrier)
-      const uint32_t mf = __ldcg(&a.farctl->minfar[splits & 1u]);
-      if (mf != 0xFFFFFFFFu && mf >= Tnew) Tnew = (mf / a.delta + 1) * a.delta;
-      uint32_t moved = 0, remaining = 0, local_min = 0xFFFFFFFFu;
-      for (uint32_t v = gtid; v < a.n; v += nthreads) {
-        const uint32_t fm = __ldcg(a.far + v);
-        if (!fm) continue;
-        uint32_t keep = 0, mv = 0, bits = fm;
-        while (bits) {
-          const uint32_t sb = __ffs(bits) - 1;
-          bits &= bits - 1;
-          const uint32_t d = __ldcg(a.D + (size_t)v * KS + sb);
-          if (d < Told) continue;  // improved below T since: expanded as near
-          if (d < Tnew) {
-            mv |= 1u << sb;
-          } else {
-            keep |= 1u << sb;
-            local_min = min(local_min, d);
-          }
-        }
-        a.far[v] = keep;
-        if (mv) a.F[sel][v] = mv;  // F[sel] is all zero after build_entries
-        moved += __popc(mv);
-        remaining += keep != 0;
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        local_min = min(local_min, __shfl_down_sync(0xffffffffu, local_min, o));
-        moved += __shfl_down_sync(0xffffffffu, moved, o);
-        remaining += __shfl_down_sync(0xffffffffu, remaining, o);
-      }
-      if (lane_id() == 0) {
-        if (local_min != 0xFFFFFFFFu) atomicMin(&a.farctl->minfar[(splits + 1) & 1u], local_min);
-        if (moved) atomicAdd(&sl->moved, moved);
-        if (remaining) atomicAdd(&sl->remaining, remaining);
-      }
-      if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-      const uint32_t mv_all = __ldcg(&sl->moved), rem_all = __ldcg(&sl->remaining);
-      if (gtid == 0) a.farctl->minfar[splits & 1u] = 0xFFFFFFFFu;
-      T = Tnew;
-      ++splits;
-      // the slot's counters are read by every CTA before they are cleared;
-      // the next split adds to them only after the next build's barrier
-      if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-      if (gtid == 0) {
-        sl->moved = 0u;
-        sl->remaining = 0u;
-      }
-      if (mv_all == 0 && rem_all == 0) break;  // nothing near, nothing far: done
-      continue;  // build entries from the moved pairs (or split again)
-    }
-    uint32_t *Fn = a.F[sel ^ 1u];
-    unsigned long long lv = 0;
-    for (uint32_t i = gwarp; i < nent; i += nwarps) lv += relax_entry<KS>(a, __ldcg(a.ent + i), Fn, T);
-    const unsigned long long bv = block_sum_u64<kBlock>(lv);
-    if (threadIdx.x == 0 && bv) atomicAdd(&sl->visits, bv);
-    if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-    visits += __ldcg(&sl->visits);
-    sel ^= 1u;
-    ++L;
-    if (L > 4u * a.n + 64u) {
-      if (gtid == 0) atomicOr(a.err, kErrLevels);
-      break;
-    }
-  }
-  // epilogue: outputs (source-major) and reach counts
-  unsigned long long nr = 0, mr = 0;
-  for (uint32_t v = gtid; v < a.n; v += nthreads) {
-    const uint32_t deg = __ldg(a.offs + v + 1) - __ldg(a.offs + v);
-    for (uint32_t s = 0; s < a.k; ++s) {
-      const uint32_t d = __ldcg(a.D + (size_t)v * KS + s);
-      a.out[s][v] = d;
-      if (d != kInfinit) {
-        ++nr;
-        mr += deg;
-      }
-    }
-  }
-  const unsigned long long bnr = block_sum_u64<kBlock>(nr);
-  const unsigned long long bmr = block_sum_u64<kBlock>(mr);
+  GridSync sync{a.bar, a.v.err, a.timeout_ns};
+  OutTable out{a.out};
+  ms::Result r;
+  if (!ms::run<KS, kBlock>(a.v, gtid, nthreads, sync, out, r)) return;
+  const unsigned long long bnr = block_sum_u64<kBlock>(r.nr);
+  const unsigned long long bmr = block_sum_u64<kBlock>(r.mr);
   if (threadIdx.x == 0) {
     atomicAdd(&a.summary->nr, bnr);
     atomicAdd(&a.summary->mr, bmr);
   }
   if (gtid == 0) {
-    a.summary->levels = L;
-    a.summary->splits = splits;
-    a.summary->visits = visits;
+    a.summary->levels = r.levels;
+    a.summary->splits = r.splits;
+    a.summary->visits = r.visits;
   }
 }
 
@@ -307,6 +83,7 @@ struct Workspace {
 constexpr size_t kOffSlots = 0, kOffFar = 256, kOffBar = 320, kOffErr = 384, kOffSummary = 448,
                  kCtrlBytes = 512;
 static_assert(4 * sizeof(Slot) <= kOffFar, "slots overlap the far control");
+static_assert(sizeof(Summary) <= kCtrlBytes - kOffSummary, "summary overflows the control block");
 
 void ws_free(void *p) {
   Workspace *w = (Workspace *)p;
@@ -390,26 +167,26 @@ int msssp_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
   GRUS_CUDA_TRY(cudaMemcpyAsync(w->srcs, hsrc, k * 4, cudaMemcpyHostToDevice, s));
   Args a;
   std::memset(&a, 0, sizeof(a));
-  a.offs = g->csr.offs;
-  a.cols = g->csr.cols;
-  a.wts = g->csr.wts;
-  a.n = (uint32_t)g->n;
-  a.k = (uint32_t)k;
-  a.srcs = w->srcs;
-  for (int i = 0; i < k; ++i) a.out[i] = outs[i];
-  a.D = w->D;
+  a.v.offs = g->csr.offs;
+  a.v.cols = g->csr.cols;
+  a.v.wts = g->csr.wts;
+  a.v.n = (uint32_t)g->n;
+  a.v.k = (uint32_t)k;
+  a.v.srcs = w->srcs;
+  a.v.D = w->D;
   const uint64_t n1 = std::max<uint64_t>(g->n, 1);
-  a.F[0] = w->masks;
-  a.F[1] = w->masks + n1;
-  a.far = w->masks + 2 * n1;
-  a.ent = w->ent;
-  a.ent_cap = w->ent_cap;
-  a.slots = (Slot *)(w->ctrl + kOffSlots);
-  a.farctl = (FarCtl *)(w->ctrl + kOffFar);
+  a.v.F[0] = w->masks;
+  a.v.F[1] = w->masks + n1;
+  a.v.far = w->masks + 2 * n1;
+  a.v.ent = w->ent;
+  a.v.ent_cap = w->ent_cap;
+  a.v.slots = (Slot *)(w->ctrl + kOffSlots);
+  a.v.minfar = (uint32_t *)(w->ctrl + kOffFar);
+  a.v.err = (uint32_t *)(w->ctrl + kOffErr);
+  a.v.delta = std::max(1u, tune_or(g->tuning.sssp_delta, kDefDelta));
+  for (int i = 0; i < k; ++i) a.out[i] = outs[i];
   a.bar = (GridBarrier *)(w->ctrl + kOffBar);
-  a.err = (uint32_t *)(w->ctrl + kOffErr);
   a.summary = (Summary *)(w->ctrl + kOffSummary);
-  a.delta = std::max(1u, tune_or(g->tuning.sssp_delta, kDefDelta));
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
   GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffSummary, 0, kCtrlBytes - kOffSummary, s));
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));

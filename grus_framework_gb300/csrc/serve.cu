@@ -12,8 +12,9 @@
 //   Big graphs (at least big_edges edges): one cluster would take many times
 //     longer than the whole GPU, so a second thread runs the whole-GPU
 //     persistent kernels (grus_bfs / grus_sssp) one launch at a time, and
-//     packs every queued BFS request on the same graph -- up to 64 -- into one
-//     multi-source launch (msbfs.cu) that writes each request's own output.
+//     packs the queued requests of one algorithm on the same graph -- up to
+//     64 BFS (msbfs.cu) or 32 SSSP (msssp.cu) -- into one multi-source launch
+//     that writes each request's own output.
 //     A graph's workspace is allocated only if free HBM covers it plus the
 //     reserve.
 // Completion is observed with an event per slot (small lane) or when the
@@ -217,13 +218,14 @@ void scheduler(grus_server *s) {
 
 // Rough device bytes of a graph's whole-GPU workspace for `algo` (BFS also
 // covers the multi-source one), used for admission before the first launch.
-size_t big_workspace_bytes(const grus_graph *g, uint32_t algo) {
+size_t big_workspace_bytes(const grus_graph *g, uint32_t algo, bool multi) {
   const size_t n = g->n, m = g->m;
+  if (algo == GRUS_ALGO_SSSP && multi) return 128 * n + 16 * n + m / 8 + (1u << 20);
   return (algo == GRUS_ALGO_SSSP ? 20 * n : 40 * n) + m / 32 + (1u << 20);
 }
 
 bool big_workspace_ready(const grus_graph *g, uint32_t algo, bool multi) {
-  if (algo == GRUS_ALGO_SSSP) return g->ws[kWsSssp] != nullptr;
+  if (algo == GRUS_ALGO_SSSP) return (multi ? g->ws[kWsMsSssp] : g->ws[kWsSssp]) != nullptr;
   return multi ? g->ws[kWsMsBfs] != nullptr : g->ws[kWsBfs] != nullptr;
 }
 
@@ -252,9 +254,10 @@ void big_scheduler(grus_server *s) {
       const Request first = s->big_pending.front();
       s->big_pending.pop_front();
       group.push_back(first);
-      if (first.algo == GRUS_ALGO_BFS) {
-        for (auto it = s->big_pending.begin(); it != s->big_pending.end() && group.size() < 64;) {
-          if (it->graph == first.graph && it->algo == GRUS_ALGO_BFS) {
+      {
+        const size_t cap = first.algo == GRUS_ALGO_BFS ? 64 : 32;
+        for (auto it = s->big_pending.begin(); it != s->big_pending.end() && group.size() < cap;) {
+          if (it->graph == first.graph && it->algo == first.algo) {
             group.push_back(*it);
             it = s->big_pending.erase(it);
           } else {
@@ -271,14 +274,13 @@ void big_scheduler(grus_server *s) {
       size_t free_b = 0, total_b = 0;
       const cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
       if (e != cudaSuccess) rc = status_from_cuda(e);
-      else if (free_b < big_workspace_bytes(g, r.algo) + s->reserve) rc = GRUS_ENOMEM;
+      else if (free_b < big_workspace_bytes(g, r.algo, multi) + s->reserve) rc = GRUS_ENOMEM;
     }
     if (rc == GRUS_OK) {
       grus_stats st;  // a stats call waits for the launch and checks its error word
-      if (r.algo == GRUS_ALGO_SSSP) {
-        rc = grus_sssp(g, r.src, r.out, &st, s->big_stream);
-      } else if (!multi) {
-        rc = grus_bfs(g, r.src, r.out, &st, s->big_stream);
+      if (!multi) {
+        rc = r.algo == GRUS_ALGO_SSSP ? grus_sssp(g, r.src, r.out, &st, s->big_stream)
+                                      : grus_bfs(g, r.src, r.out, &st, s->big_stream);
       } else {
         uint32_t srcs[64];
         uint32_t *outs[64];
@@ -286,7 +288,9 @@ void big_scheduler(grus_server *s) {
           srcs[i] = group[i].src;
           outs[i] = group[i].out;
         }
-        rc = msbfs_run(g, srcs, (int)group.size(), outs, &st, s->big_stream);
+        rc = r.algo == GRUS_ALGO_SSSP
+                 ? msssp_run(g, srcs, (int)group.size(), outs, &st, s->big_stream)
+                 : msbfs_run(g, srcs, (int)group.size(), outs, &st, s->big_stream);
       }
     }
     const auto now = Clock::now();

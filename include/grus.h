@@ -268,6 +268,12 @@ typedef struct grus_batch_config {
   uint32_t workers;      /* 0 = as many as fit */
   uint32_t huge_degree;  /* hub chunking threshold */
   uint32_t sssp_delta;   /* SSSP bucket width */
+  uint32_t group_sources;/* SSSP queries on one graph packed per multi-source
+                            task (1..32; default 1 = no packing: on a 16-CTA
+                            worker a pack of 8 costs about 3.3 single
+                            queries, so packing pays only when workers would
+                            otherwise idle, e.g. many queries on few small
+                            graphs) */
 } grus_batch_config;
 
 typedef struct grus_batch grus_batch;
@@ -290,8 +296,8 @@ GRUS_API int grus_batch_free(grus_batch *b);
  * is free, allocating a slot's state only if free HBM covers it plus
  * hbm_reserve_bytes; admitted queries overlap on the device.  Big graphs: a
  * second thread runs whole-GPU persistent launches one at a time, and packs
- * every queued BFS query on the same graph (up to 64) into one multi-source
- * launch; a graph's workspace is allocated only if free HBM covers it plus
+ * the queued queries of one algorithm on the same graph (up to 64 BFS or 32
+ * SSSP) into one multi-source launch; a graph's workspace is allocated only if free HBM covers it plus
  * the reserve.  Latency is measured from submit to observed completion on the
  * host clock. */
 typedef struct grus_server grus_server;
@@ -316,8 +322,8 @@ typedef struct grus_server_stats {
   uint64_t submitted, admitted, completed, pending, rejected;
   uint32_t slots, slots_ready;
   uint64_t big_launches;     /* whole-GPU launches of the big-graph lane */
-  uint64_t big_queries;      /* queries they served (BFS queries on one graph
-                                share a multi-source launch) */
+  uint64_t big_queries;      /* queries they served (queries of one algorithm
+                                on one graph share a multi-source launch) */
 } grus_server_stats;
 
 GRUS_API int grus_server_create(grus_graph *const *graphs, int ngraphs,

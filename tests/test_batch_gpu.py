@@ -107,3 +107,34 @@ def test_batch_single_worker_high_diameter(grus, oracle_mod):
         b.run([(0, grus.ALGO_BFS, 41)], out, [0], stats=True)
         assert np.array_equal(out.cpu().numpy().view(np.uint32), grus.bfs(g, 41))
         b.free()
+
+
+@pytest.mark.parametrize("group", [1, 5, 16, 32])
+def test_batch_sssp_groups(grus, graphs, group):
+    """SSSP queries on one graph are packed `group` at a time into
+    multi-source tasks (1 = no packing); every result equals the single
+    query, with plain launches and CUDA-graph replays, and repeated sources."""
+    torch = pytest.importorskip("torch")
+    b = grus.Batch(graphs, group_sources=group)
+    assert b.info()["group_sources"] == group
+    rng = np.random.default_rng(group)
+    queries = []
+    for gi in (0, 2, 3, 6):
+        for _ in range(int(rng.integers(1, 40))):
+            queries.append((gi, grus.ALGO_SSSP, int(rng.integers(graphs[gi].n))))
+    queries.append((2, grus.ALGO_SSSP, queries[-1][2]))  # a repeated source
+    queries += make_queries(grus, graphs, 20, 77)  # mixed BFS/SSSP singles
+    for use_graph in (False, True, True):
+        offs, total = b.layout(queries)
+        out = torch.full((total,), -3, dtype=torch.int32, device="cuda")
+        b.run(queries, out, offs, use_graph=use_graph, stats=True)
+        res = out.cpu().numpy().view(np.uint32)
+        for q, o in zip(queries, offs):
+            ref = reference(grus, graphs, q)
+            assert np.array_equal(res[o:o + len(ref)], ref), (group, use_graph, q)
+    b.free()
+
+
+def test_batch_rejects_bad_group_size(grus, graphs):
+    with pytest.raises(grus.GrusError):
+        grus.Batch(graphs, group_sources=33)

@@ -68,9 +68,9 @@ def test_server_rejects_bad_submissions(grus, graphs):
 
 
 def test_server_big_lane_groups_bfs_and_matches_alone(grus, graphs):
-    """With big_edges=1 every graph is served by the whole-GPU lane: queued BFS
-    queries on one graph share multi-source launches, SSSP runs alone, and each
-    result equals the query run alone."""
+    """With big_edges=1 every graph is served by the whole-GPU lane: queued
+    queries of one algorithm on one graph share multi-source launches, and
+    each result equals the query run alone."""
     torch = pytest.importorskip("torch")
     srv = grus.Server(graphs, slots=2, big_edges=1)
     rng = np.random.default_rng(7)
@@ -91,7 +91,7 @@ def test_server_big_lane_groups_bfs_and_matches_alone(grus, graphs):
         assert np.array_equal(out.cpu().numpy().view(np.uint32), alone)
     st = srv.stats()
     assert st["big_queries"] == len(reqs) and st["completed"] == len(reqs)
-    assert st["big_launches"] < len(reqs)  # BFS queries were packed
+    assert st["big_launches"] < len(reqs)  # queries were packed
     srv.close()
 
 
