@@ -22,8 +22,8 @@ events.
                   [--workload NAME] [--scale S]
 
 Other workloads (`--workload`): sssp-rmat22, cc-rmat22, pagerank-rmat24
-(directed), bfs-grid4096, msbfs-rmat23 (64 sources), msssp-rmat22 (32
-sources).  `--scale` overrides
+(directed), bfs-grid4096, bfs-rmat26-managed (managed memory, device budget
+half the CSR bytes), msbfs-rmat23 (64 sources), msssp-rmat22 (32 sources).  `--scale` overrides
 the RMAT scale (or the grid side as a power of two) for small profiling runs.
 
 `--impl reference` times the CPU path (the reference has no host traversal;
@@ -70,6 +70,11 @@ WORKLOADS = {
     "msbfs-rmat23": dict(algo="msbfs", graph="rmat", scale=23, edge_factor=16, seed=4,
                          symmetric=True, weighted=False, kernel="msbfs_persistent", sources=64,
                          metric="GTEPS (64-source BFS in one launch, RMAT-23 symmetrised)"),
+    "bfs-rmat26-managed": dict(algo="bfs", graph="rmat", scale=26, edge_factor=16, seed=3,
+                               symmetric=True, weighted=False, kernel="bfs_persistent",
+                               managed=True, budget_fraction=0.5,
+                               metric="GTEPS (single-query BFS, RMAT-26 symmetrised, managed "
+                                      "memory, device budget 50% of the CSR bytes)"),
     "msssp-rmat22": dict(algo="msssp", graph="rmat", scale=22, edge_factor=16, seed=2,
                          symmetric=True, weighted=True, kernel="msssp_persistent", sources=32,
                          metric="GTEPS (32-source SSSP in one launch, RMAT-22 symmetrised, w in [1,255])"),
@@ -304,8 +309,17 @@ def run_grus(args, dist, rank, local):
         g = grus.Graph.grid2d(side, side, w.get("seed", 0))
         src = grid_source(side)
     else:
+        budget = 0
+        if w.get("managed"):
+            # the budget is a fraction of the CSR bytes, known once the graph exists
+            g0 = grus.Graph.rmat(w["scale"], w["edge_factor"], w["seed"], symmetric=w["symmetric"],
+                                 weighted=w["weighted"], relabel=True)
+            budget = int(w["budget_fraction"] * (4 * (g0.n + 1) + 4 * g0.m))
+            g0.free()
+            w["budget_bytes"] = budget
         g = grus.Graph.rmat(w["scale"], w["edge_factor"], w["seed"], symmetric=w["symmetric"],
-                            weighted=w["weighted"], relabel=True)
+                            weighted=w["weighted"], relabel=True, managed=bool(w.get("managed")),
+                            budget_bytes=budget)
         src = g.max_degree_vertex
     n, m = g.n, g.m
     stream = torch.cuda.Stream()
@@ -438,7 +452,9 @@ def run_grus(args, dist, rank, local):
             "config": cfg,
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
-                    "note": "public API call with a pinned host output buffer; graph resident in HBM"},
+                    "note": "public API call with a pinned host output buffer; graph " + (
+                        "in managed memory, device budget %d bytes" % w["budget_bytes"]
+                        if w.get("managed") else "resident in HBM")},
             "gpu_launches": launches * args.steps,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,

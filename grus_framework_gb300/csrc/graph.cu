@@ -221,6 +221,28 @@ int apply_mem_policy(grus_graph *g, cudaStream_t s) {
     const uint64_t pc = std::min(cb, left);
     if (pc) GRUS_CUDA_TRY(cudaMemPrefetchAsync(g->csr.cols, pc, loc, 0, s));
   }
+  // whatever lies beyond the budget starts on the host, wherever it was
+  // written (a graph generated on the device is first touched there)
+  if (g->budget_bytes) {
+    cudaMemLocation host{};
+    host.type = cudaMemLocationTypeHost;
+    host.id = 0;
+    const uint64_t po2 = std::min(ob, budget);
+    uint64_t left2 = budget - po2;
+    uint64_t pc2 = 0, pw2 = 0;
+    if (wb) {
+      pc2 = std::min(cb, left2 / 2);
+      pw2 = std::min(wb, left2 - pc2);
+    } else {
+      pc2 = std::min(cb, left2);
+    }
+    if (ob > po2)
+      GRUS_CUDA_TRY(cudaMemPrefetchAsync((char *)g->csr.offs + po2, ob - po2, host, 0, s));
+    if (cb > pc2)
+      GRUS_CUDA_TRY(cudaMemPrefetchAsync((char *)g->csr.cols + pc2, cb - pc2, host, 0, s));
+    if (wb > pw2)
+      GRUS_CUDA_TRY(cudaMemPrefetchAsync((char *)g->csr.wts + pw2, wb - pw2, host, 0, s));
+  }
   GRUS_CUDA_TRY(cudaStreamSynchronize(s));
   if (g->budget_bytes && !g->balloon) {
     size_t free_b = 0, total_b = 0;
