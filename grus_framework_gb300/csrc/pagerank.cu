@@ -15,8 +15,9 @@
 // one fused pass: gather c over in-edges, form r, write c_next (and r on the
 // last iteration).  Per 256-vertex tile, in-degree is binned:
 //   >= kCtaTh (1024) : whole CTA strides the list, block reduction
-//   >= 32            : one warp, shuffle reduction
-//   <  32            : one thread, loads unrolled four wide
+//   >= 32            : one warp, loads four wide, shuffle reduction
+//   <  32            : the warp's short lists laid end to end, one edge per
+//                      lane, segmented warp scan (every lane busy)
 // Per-thread partial sums over more than kKahanTh terms use compensated
 // (Kahan-Babuska) summation; reductions across lanes are pairwise trees.
 // The contribution arrays sit in an L2 persisting window.
@@ -76,17 +77,82 @@ __device__ __forceinline__ void finish(const Args &a, uint32_t v, float sum, flo
   if (last) a.rank[v] = r;
 }
 
+// Strided gather of one list: four source ids, then their four
+// contributions, are loaded before they are added (four load chains in
+// flight per thread).
 __device__ __forceinline__ float gather_seq(const Args &a, const float *cs, uint32_t b,
                                             uint32_t e, uint32_t step) {
   if (b >= e) return 0.f;
-  if ((e - b) <= kKahanTh * step) {
-    float s = 0.f;
-    for (uint32_t x = b; x < e; x += step) s += __ldcg(cs + __ldg(a.tcols + x));
-    return s;
-  }
+  const bool comp = (e - b) > kKahanTh * step;
   KSum k;
-  for (uint32_t x = b; x < e; x += step) k.add(__ldcg(cs + __ldg(a.tcols + x)));
-  return k.value();
+  float s = 0.f;
+  uint32_t x = b;
+  for (; x + 3 * step < e; x += 4 * step) {
+    const uint32_t u0 = __ldg(a.tcols + x), u1 = __ldg(a.tcols + x + step);
+    const uint32_t u2 = __ldg(a.tcols + x + 2 * step), u3 = __ldg(a.tcols + x + 3 * step);
+    const float f0 = __ldcg(cs + u0), f1 = __ldcg(cs + u1);
+    const float f2 = __ldcg(cs + u2), f3 = __ldcg(cs + u3);
+    if (comp) {
+      k.add(f0);
+      k.add(f1);
+      k.add(f2);
+      k.add(f3);
+    } else {
+      s += (f0 + f1) + (f2 + f3);
+    }
+  }
+  for (; x < e; x += step) {
+    const float f = __ldcg(cs + __ldg(a.tcols + x));
+    if (comp) k.add(f);
+    else s += f;
+  }
+  return comp ? k.value() : s;
+}
+
+// The short lists (< 32 in-edges) of a warp's vertices, laid end to end:
+// lane k of a step takes edge k of the concatenation (coalesced source-id
+// loads, every lane busy), a segmented warp scan sums each vertex's run
+// within the step (a fixed pairwise order), and the owning lane adds its
+// run's sum.  Returns the full sum for the calling lane's vertex.
+__device__ __forceinline__ float gather_short(const Args &a, const float *cs, uint32_t beg,
+                                              uint32_t deg) {
+  const uint32_t lane = lane_id();
+  uint32_t incl = deg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((int)lane >= o) incl += t;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  const uint32_t excl = incl - deg;
+  KSum acc;
+  for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+    const uint32_t k = k0 + lane;
+    int j = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const uint32_t pv = __shfl_sync(0xffffffffu, incl, j + step - 1);
+      if (pv <= k) j += step;
+    }
+    const uint32_t ob = __shfl_sync(0xffffffffu, beg, j);
+    const uint32_t oe = __shfl_sync(0xffffffffu, excl, j);
+    float v = k < total ? __ldcg(cs + __ldg(a.tcols + ob + (k - oe))) : 0.f;
+    bool head = lane == 0 || k == oe;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float tv = __shfl_up_sync(0xffffffffu, v, o);
+      const bool th = __shfl_up_sync(0xffffffffu, head, o);
+      if ((int)lane >= o && !head) {
+        v += tv;
+        head = th;
+      }
+    }
+    // this lane's run within the step ends at min(incl, k0 + 32) - 1
+    const uint32_t rs = max(excl, k0), re = min(incl, k0 + 32);
+    const float t = __shfl_sync(0xffffffffu, v, rs < re ? re - 1 - k0 : 0);
+    if (rs < re) acc.add(t);
+  }
+  return acc.value();
 }
 
 __global__ void __launch_bounds__(kBlock) pr_persistent(Args a) {
@@ -111,14 +177,12 @@ __global__ void __launch_bounds__(kBlock) pr_persistent(Args a) {
         end = __ldg(a.toffs + v + 1);
       }
       bool done = v >= a.n;
-      // CTA-cooperative for very high in-degree
-      while (true) {
-        if (threadIdx.x == 0) s_owner = 0xFFFFFFFFu;
-        __syncthreads();
-        if (!done && end - beg >= kCtaTh) s_owner = threadIdx.x;
+      // CTA-cooperative for very high in-degree (one block vote per tile
+      // when no vertex qualifies)
+      while (__syncthreads_or(!done && end - beg >= kCtaTh)) {
+        if (!done && end - beg >= kCtaTh) s_owner = threadIdx.x;  // any qualifying thread wins
         __syncthreads();
         const uint32_t owner = s_owner;
-        if (owner == 0xFFFFFFFFu) break;
         if (threadIdx.x == owner) {
           s_v = v;
           s_beg = beg;
@@ -149,20 +213,9 @@ __global__ void __launch_bounds__(kBlock) pr_persistent(Args a) {
         const float tot = warp_sum(gather_seq(a, cs, wb + lane, we, 32));
         if ((int)lane == leader) finish(a, wv, tot, cn, last);
       }
-      // one thread per short list, loads four wide
-      if (!done) {
-        float s = 0.f;
-        uint32_t x = beg;
-        for (; x + 4 <= end; x += 4) {
-          const uint32_t u0 = __ldg(a.tcols + x), u1 = __ldg(a.tcols + x + 1);
-          const uint32_t u2 = __ldg(a.tcols + x + 2), u3 = __ldg(a.tcols + x + 3);
-          const float f0 = __ldcg(cs + u0), f1 = __ldcg(cs + u1);
-          const float f2 = __ldcg(cs + u2), f3 = __ldcg(cs + u3);
-          s += (f0 + f1) + (f2 + f3);
-        }
-        for (; x < end; ++x) s += __ldcg(cs + __ldg(a.tcols + x));
-        finish(a, v, s, cn, last);
-      }
+      // the warp's short lists, end to end
+      const float s = gather_short(a, cs, beg, done ? 0u : end - beg);
+      if (!done) finish(a, v, s, cn, last);
     }
     if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
   }
