@@ -8,17 +8,22 @@
 // sources race.  Here every relaxation is atomicMin, so the result is the
 // unique fixpoint -- Dijkstra's distances -- whatever the schedule.
 //
-// Per iteration the near frontier (vertices whose distance improved and is
-// below the threshold T) is expanded with the degree-binned mappings of
-// expand.cuh.  An improved vertex v goes
-//   * to the next near frontier if dist(v) < T (deduplicated by a rotating
-//     bitmap), else
-//   * to the far pile (deduplicated by a far bitmap).
-// When the near frontier empties, T advances by Delta and the far pile is
-// split: entries below the old T were already expanded and are dropped,
-// entries below the new T become the near frontier, the rest stay.  If a
-// split yields nothing, T jumps to the bucket of the smallest far distance.
-// Every wait is a bounded grid barrier (grus_internal.cuh).
+// The near and far sets are bitmaps (one bit per vertex):
+//   N[L & 1]  vertices to expand at level L (improved below the threshold T)
+//   N[~L & 1] vertices improved below T during level L
+//   F         vertices improved to a distance >= T (far)
+// A level
+//   1. compacts N[L & 1] into binned work lists (degree < huge: vertex queue;
+//      degree >= huge: 1024-edge chunks), clearing the bitmap as it reads it,
+//      with one queue reservation per CTA (block scan of the counts);
+//   2. expands the lists with the degree-binned mappings of expand.cuh; a
+//      relaxation that beats the distance it read lowers it with a
+//      non-returning atomicMin and sets v's bit in N[~L & 1] (new distance < T)
+//      or F -- also a reduction, so the relaxation path waits on no atomic.
+// When a level finds nothing to expand, T advances by Delta (or jumps to the
+// bucket of the smallest far distance) and F is scanned: vertices below the
+// old T were expanded as near since and are dropped, vertices below the new T
+// move to N[L & 1], the rest stay.  Every wait is a bounded grid barrier.
 #include <algorithm>
 #include <cstring>
 
@@ -29,8 +34,8 @@ namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr uint32_t kDefHuge = 1024;
-constexpr uint32_t kDefDelta = 96;
+constexpr uint32_t kDefHuge = 256;
+constexpr uint32_t kDefDelta = 192;
 
 struct Slot {
   uint32_t qcount, ccount;
@@ -38,11 +43,11 @@ struct Slot {
   uint32_t pad[4];
 };
 
-// Far-pile control.  minfar is double-buffered by split parity so that the
+// Far-set control.  minfar is double-buffered by split parity so that the
 // value every CTA reads at the start of split k (written during split k-1) is
 // never the one being reset or reduced during split k.
 struct FarCtl {
-  uint32_t count[2];
+  uint32_t moved, remaining;  // of the current split
   uint32_t minfar[2];
 };
 
@@ -66,11 +71,10 @@ struct Args {
   uint32_t n, W;
   uint32_t src;
   uint32_t *dist;
-  uint32_t *inq[3];
-  uint32_t *farbm;
-  uint32_t *queue[2];
-  uint4 *chunks[2];
-  uint32_t *far[2];
+  uint32_t *near[2];      // W words each
+  uint32_t *farbm;        // W words
+  uint32_t *queue;        // this level's vertex queue
+  uint4 *chunks;          // this level's hub chunks
   uint32_t queue_cap, chunk_cap;
   Slot *slots;
   FarCtl *farctl;
@@ -85,10 +89,9 @@ struct Args {
 struct Workspace {
   uint32_t W = 0;
   uint32_t *dist = nullptr;
-  uint32_t *bitmaps = nullptr;  // 4 * Wp words: inq[3], farbm
+  uint32_t *bitmaps = nullptr;  // 3 * Wp words: near[2], farbm
   size_t bitmap_bytes = 0;
-  uint32_t *queues = nullptr;   // 2n
-  uint32_t *far = nullptr;      // 2n
+  uint32_t *queues = nullptr;   // n
   uint4 *chunks = nullptr;
   uint32_t chunk_cap = 0;
   char *ctrl = nullptr, *ctrl_host = nullptr;
@@ -106,7 +109,6 @@ void ws_free(void *p) {
   cudaFree(w->dist);
   cudaFree(w->bitmaps);
   cudaFree(w->queues);
-  cudaFree(w->far);
   cudaFree(w->chunks);
   cudaFree(w->ctrl);
   cudaFree(w->trace);
@@ -125,14 +127,13 @@ int ws_get(grus_graph *g, Workspace **out) {
   Workspace *w = new Workspace();
   w->W = (uint32_t)((g->n + 31) / 32);
   const uint64_t Wp = ((uint64_t)w->W + 31) / 32 * 32;
-  w->bitmap_bytes = 4 * Wp * 4;
+  w->bitmap_bytes = 3 * Wp * 4;
   const uint32_t huge = tune_or(g->tuning.huge_degree, kDefHuge);
   w->chunk_cap = (uint32_t)std::min<uint64_t>(g->m / kChunk + g->m / huge + 2, 0x7FFFFFFFull);
   const uint64_t n1 = std::max<uint64_t>(g->n, 1);
   cudaError_t e = cudaMalloc(&w->bitmaps, w->bitmap_bytes);
-  if (e == cudaSuccess) e = cudaMalloc(&w->queues, 2 * n1 * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&w->far, 2 * n1 * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&w->chunks, 2ull * w->chunk_cap * sizeof(uint4));
+  if (e == cudaSuccess) e = cudaMalloc(&w->queues, n1 * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&w->chunks, (uint64_t)w->chunk_cap * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
   if (e == cudaSuccess) e = cudaMemset(w->ctrl, 0, kCtrlBytes);
   if (e == cudaSuccess) e = cudaMallocHost(&w->ctrl_host, kCtrlBytes);
@@ -152,140 +153,174 @@ int ws_get(grus_graph *g, Workspace **out) {
   return GRUS_OK;
 }
 
-// Marks v for the next near frontier (once per level) and queues it.
-__device__ __forceinline__ void to_near(const Args &a, uint32_t v, uint32_t *inq_next,
-                                        uint32_t *qnext, uint4 *cnext, Slot *nx) {
-  const uint32_t w = v >> 5, bit = 1u << (v & 31u);
-  if (__ldcg(inq_next + w) & bit) return;
-  if (atomicOr(inq_next + w, bit) & bit) return;
-  const uint32_t b = __ldg(a.offs + v), e = __ldg(a.offs + v + 1);
-  if (!push_binned(v, b, e, a.huge, qnext, &nx->qcount, a.queue_cap, cnext, &nx->ccount,
-                   a.chunk_cap))
-    atomicOr(a.err, kErrOverflow);
-}
-
 struct RelaxVisitor {
   const Args *a;
   uint32_t T;
-  uint32_t *inq_next, *qnext, *farp;
-  uint32_t *farcount;
-  uint4 *cnext;
-  Slot *nx;
+  uint32_t *nnext;
   unsigned long long visits;
 
   using aux_t = uint32_t;
 
   __device__ __forceinline__ uint32_t aux(uint32_t v) const { return __ldcg(a->dist + v); }
+  // A reduction lowers dist(v) and another marks v; neither is waited for.
+  // If another thread lowered dist(v) further meanwhile, v is marked all the
+  // same (a bit), costing at most one redundant expansion.
   __device__ __forceinline__ void edge(uint32_t, uint32_t du, uint32_t x) {
     ++visits;
     const uint32_t v = __ldg(a->cols + x);
     const uint32_t nd = du + __ldg(a->wts + x);
     if (nd >= __ldcg(a->dist + v)) return;
-    // a reduction: the old value is not waited for.  If another thread
-    // lowered dist(v) further meanwhile, v is still marked below (the
-    // bitmaps deduplicate), costing at most one redundant expansion.
     atomicMin(a->dist + v, nd);
-    if (nd < T) {
-      to_near(*a, v, inq_next, qnext, cnext, nx);
-    } else {
-      const uint32_t w = v >> 5, bit = 1u << (v & 31u);
-      if (__ldcg(a->farbm + w) & bit) return;
-      if (atomicOr(a->farbm + w, bit) & bit) return;
-      const uint32_t pos = agg_reserve(farcount);
-      if (pos < a->queue_cap) farp[pos] = v;
-      else atomicOr(a->err, kErrOverflow);
-    }
+    atomicOr((nd < T ? nnext : a->farbm) + (v >> 5), 1u << (v & 31u));
   }
 };
+
+// Step 1: the set bits of `bm` become work: degree < huge into the vertex
+// queue (one reservation per CTA), degree >= huge into 1024-edge chunks.
+// Every word is cleared as it is read.  Each CTA owns a contiguous range of
+// words.
+__device__ __forceinline__ void bitmap_to_lists(const Args &a, uint32_t *bm, Slot *sl) {
+  __shared__ uint32_t s_base;
+  const uint32_t per = (a.W + gridDim.x - 1) / gridDim.x;
+  const uint32_t w0 = min(a.W, blockIdx.x * per), w1 = min(a.W, w0 + per);
+  for (uint32_t base = w0; base < w1; base += kBlock) {
+    const uint32_t w = base + threadIdx.x;
+    uint32_t word = w < w1 ? __ldcg(bm + w) : 0u;
+    if (word) bm[w] = 0u;
+    uint32_t cnt = 0;
+    for (uint32_t bits = word; bits; bits &= bits - 1) {
+      const uint32_t v = w * 32 + (__ffs(bits) - 1);
+      const uint32_t b = __ldg(a.offs + v), e = __ldg(a.offs + v + 1);
+      const uint32_t d = e - b;
+      if (d == 0) continue;
+      if (d < a.huge) {
+        ++cnt;
+      } else {
+        const uint32_t nch = (d + kChunk - 1) / kChunk;
+        const uint32_t pos = atomicAdd(&sl->ccount, nch);
+        if (pos + nch > a.chunk_cap) {
+          atomicOr(a.err, kErrOverflow);
+        } else {
+          for (uint32_t k = 0; k < nch; ++k)
+            a.chunks[pos + k] = make_uint4(v, b + k * kChunk, min(e, b + (k + 1) * kChunk), 0u);
+        }
+      }
+    }
+    uint32_t total = 0;
+    uint32_t at = block_exclusive_scan<kBlock>(cnt, &total);
+    if (threadIdx.x == 0 && total) s_base = atomicAdd(&sl->qcount, total);
+    __syncthreads();
+    if (cnt) {
+      at += s_base;
+      for (uint32_t bits = word; bits; bits &= bits - 1) {
+        const uint32_t v = w * 32 + (__ffs(bits) - 1);
+        const uint32_t d = __ldg(a.offs + v + 1) - __ldg(a.offs + v);
+        if (d == 0 || d >= a.huge) continue;
+        if (at < a.queue_cap) a.queue[at] = v;
+        else atomicOr(a.err, kErrOverflow);
+        ++at;
+      }
+    }
+    __syncthreads();
+  }
+}
 
 __global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
   // prologue: distances to INFINIT, bitmaps and control words to zero
   for (uint32_t i = gtid; i < a.n; i += nthreads) a.dist[i] = kInfinit;
-  {
-    const uint32_t words = (uint32_t)(a.farbm - a.inq[0]) + a.W;
-    for (uint32_t i = gtid; i < words; i += nthreads) a.inq[0][i] = 0u;
-    if (gtid < 4 * sizeof(Slot) / 4) ((uint32_t *)a.slots)[gtid] = 0u;
-    if (gtid < sizeof(FarCtl) / 4) ((uint32_t *)a.farctl)[gtid] = 0u;
+  for (uint32_t i = gtid; i < a.W; i += nthreads) {
+    a.near[0][i] = 0u;
+    a.near[1][i] = 0u;
+    a.farbm[i] = 0u;
+  }
+  if (gtid < 4 * sizeof(Slot) / 4) ((uint32_t *)a.slots)[gtid] = 0u;
+  if (gtid < sizeof(FarCtl) / 4) ((uint32_t *)a.farctl)[gtid] = 0u;
+  if (gtid == 0) {
+    a.farctl->minfar[0] = 0xFFFFFFFFu;
+    a.farctl->minfar[1] = 0xFFFFFFFFu;
   }
   if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
   if (gtid == 0) {
     a.dist[a.src] = 0;
-    const uint32_t b = __ldg(a.offs + a.src), e = __ldg(a.offs + a.src + 1);
-    if (!push_binned(a.src, b, e, a.huge, a.queue[0], &a.slots[0].qcount, a.queue_cap,
-                     a.chunks[0], &a.slots[0].ccount, a.chunk_cap))
-      atomicOr(a.err, kErrOverflow);
+    a.near[0][a.src >> 5] = 1u << (a.src & 31u);
   }
   if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
 
-  uint32_t L = 0, T = a.delta, fsel = 0, splits = 0;
+  uint32_t L = 0, T = a.delta, splits = 0;
   unsigned long long visits = 0;
   if (gtid == 0 && a.trace) a.trace[0] = LevelTrace{global_timer_ns(), 0ull, 1u, 0u};
   while (true) {
-    Slot *cur = a.slots + (L & 3u), *nx = a.slots + ((L + 1) & 3u);
-    uint32_t *inq_next = a.inq[(L + 1) % 3];
-    uint32_t *inq_clr = a.inq[(L + 2) % 3];
-    for (uint32_t i = gtid; i < a.W; i += nthreads) inq_clr[i] = 0u;
+    Slot *sl = a.slots + (L & 3u);
     if (gtid < sizeof(Slot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[gtid] = 0u;
-    const uint32_t qc = min(__ldcg(&cur->qcount), a.queue_cap);
-    const uint32_t cc = min(__ldcg(&cur->ccount), a.chunk_cap);
-    RelaxVisitor vis{&a, T, inq_next, a.queue[(L + 1) & 1u], a.far[fsel],
-                     &a.farctl->count[fsel], a.chunks[(L + 1) & 1u], nx, 0ull};
-    expand_binned<kBlock>(a.offs, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, vis);
-    const unsigned long long bv = block_sum_u64<kBlock>(vis.visits);
-    if (threadIdx.x == 0 && bv) atomicAdd(&nx->visits, bv);
+    uint32_t *ncur = a.near[L & 1u], *nnext = a.near[(L + 1) & 1u];
+    bitmap_to_lists(a, ncur, sl);
     if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-    const unsigned long long lv = __ldcg(&nx->visits);
-    visits += lv;
-    ++L;
-    bool done = false;
-    // near frontier empty: advance the threshold and split the far pile
-    while (__ldcg(&nx->qcount) + __ldcg(&nx->ccount) == 0) {
-      const uint32_t fc = min(__ldcg(&a.farctl->count[fsel]), a.queue_cap);
-      if (fc == 0) {
-        done = true;
-        break;
-      }
+    const uint32_t qc = min(__ldcg(&sl->qcount), a.queue_cap);
+    const uint32_t cc = min(__ldcg(&sl->ccount), a.chunk_cap);
+    if (qc + cc == 0) {
+      // nothing near: advance the threshold and split the far set into ncur
       const uint32_t Told = T;
       uint32_t Tnew = T + a.delta;
       const uint32_t mf = __ldcg(&a.farctl->minfar[splits & 1u]);
-      if (splits && mf != 0xFFFFFFFFu && mf >= Tnew) Tnew = (mf / a.delta + 1) * a.delta;
-      if (gtid == 0) {
-        a.farctl->count[fsel ^ 1u] = 0u;
-        a.farctl->minfar[(splits + 1) & 1u] = 0xFFFFFFFFu;
-      }
-      if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-      const uint32_t *fp = a.far[fsel];
-      uint32_t *kp = a.far[fsel ^ 1u];
-      uint32_t local_min = 0xFFFFFFFFu;
-      for (uint32_t i = gtid; i < fc; i += nthreads) {
-        const uint32_t v = __ldcg(fp + i);
-        const uint32_t d = __ldcg(a.dist + v);
-        const uint32_t w = v >> 5, bit = 1u << (v & 31u);
-        if (d < Told) {
-          atomicAnd(a.farbm + w, ~bit);  // already expanded from the near frontier
-        } else if (d < Tnew) {
-          atomicAnd(a.farbm + w, ~bit);
-          to_near(a, v, inq_next, a.queue[L & 1u], a.chunks[L & 1u], nx);
-        } else {
-          const uint32_t pos = agg_reserve(&a.farctl->count[fsel ^ 1u]);
-          kp[pos] = v;
-          local_min = min(local_min, d);
+      if (mf != 0xFFFFFFFFu && mf >= Tnew) Tnew = (mf / a.delta + 1) * a.delta;
+      uint32_t moved = 0, remaining = 0, local_min = 0xFFFFFFFFu;
+      for (uint32_t w = gtid; w < a.W; w += nthreads) {
+        const uint32_t fw = __ldcg(a.farbm + w);
+        if (!fw) continue;
+        uint32_t keep = 0, mv = 0;
+        for (uint32_t bits = fw; bits; bits &= bits - 1) {
+          const uint32_t b = __ffs(bits) - 1;
+          const uint32_t d = __ldcg(a.dist + w * 32 + b);
+          if (d < Told) continue;  // improved below T since: expanded as near
+          if (d < Tnew) {
+            mv |= 1u << b;
+          } else {
+            keep |= 1u << b;
+            local_min = min(local_min, d);
+          }
         }
+        a.farbm[w] = keep;
+        if (mv) ncur[w] = mv;  // ncur is all zero after bitmap_to_lists
+        moved += __popc(mv);
+        remaining += keep != 0;
       }
-      for (int o = 16; o > 0; o >>= 1)
+      for (int o = 16; o > 0; o >>= 1) {
         local_min = min(local_min, __shfl_down_sync(0xffffffffu, local_min, o));
-      if (lane_id() == 0 && local_min != 0xFFFFFFFFu)
-        atomicMin(&a.farctl->minfar[(splits + 1) & 1u], local_min);
-      T = Tnew;
-      fsel ^= 1u;
-      ++splits;
+        moved += __shfl_down_sync(0xffffffffu, moved, o);
+        remaining += __shfl_down_sync(0xffffffffu, remaining, o);
+      }
+      if (lane_id() == 0) {
+        if (local_min != 0xFFFFFFFFu) atomicMin(&a.farctl->minfar[(splits + 1) & 1u], local_min);
+        if (moved) atomicAdd(&a.farctl->moved, moved);
+        if (remaining) atomicAdd(&a.farctl->remaining, remaining);
+      }
       if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+      const uint32_t mv_all = __ldcg(&a.farctl->moved), rem_all = __ldcg(&a.farctl->remaining);
+      if (gtid == 0) a.farctl->minfar[splits & 1u] = 0xFFFFFFFFu;  // read by all before the barrier
+      T = Tnew;
+      ++splits;
+      // every CTA has read the counters before they are cleared; the next
+      // split adds to them only after the next compaction's barrier
+      if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+      if (gtid == 0) {
+        a.farctl->moved = 0u;
+        a.farctl->remaining = 0u;
+      }
+      if (mv_all == 0 && rem_all == 0) break;  // nothing near, nothing far: done
+      continue;  // compact the moved vertices (or split again)
     }
+    RelaxVisitor vis{&a, T, nnext, 0ull};
+    expand_binned<kBlock>(a.offs, a.queue, qc, a.chunks, cc, vis);
+    const unsigned long long bv = block_sum_u64<kBlock>(vis.visits);
+    if (threadIdx.x == 0 && bv) atomicAdd(&sl->visits, bv);
+    if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+    const unsigned long long lv = __ldcg(&sl->visits);
+    visits += lv;
+    ++L;
     if (gtid == 0 && a.trace && L < (uint32_t)kMaxTrace)
       a.trace[L] = LevelTrace{global_timer_ns(), lv, qc + cc, splits};
-    if (done) break;
     if (L > 4u * a.n + 64u) {
       if (gtid == 0) atomicOr(a.err, kErrLevels);
       break;
@@ -348,14 +383,11 @@ extern "C" int grus_sssp(grus_graph *g, uint32_t src, uint32_t *dist,
   a.src = src;
   a.dist = dev_out ? dist : w->dist;
   const uint64_t Wp = ((uint64_t)w->W + 31) / 32 * 32;
-  for (int i = 0; i < 3; ++i) a.inq[i] = w->bitmaps + i * Wp;
-  a.farbm = w->bitmaps + 3 * Wp;
-  a.queue[0] = w->queues;
-  a.queue[1] = w->queues + g->n;
-  a.far[0] = w->far;
-  a.far[1] = w->far + g->n;
-  a.chunks[0] = w->chunks;
-  a.chunks[1] = w->chunks + w->chunk_cap;
+  a.near[0] = w->bitmaps;
+  a.near[1] = w->bitmaps + Wp;
+  a.farbm = w->bitmaps + 2 * Wp;
+  a.queue = w->queues;
+  a.chunks = w->chunks;
   a.queue_cap = (uint32_t)g->n;
   a.chunk_cap = w->chunk_cap;
   a.slots = (Slot *)(w->ctrl + kOffSlots);
