@@ -10,8 +10,8 @@
 // Algorithms:
 //   BFS  : push levels with the degree-binned expansion of expand.cuh (CTA /
 //          warp / gather mappings, hub chunks), visited bitmap claims.
-//   SSSP : the near/far label-correcting scheme of sssp.cu (atomicMin,
-//          Delta buckets), scoped to the cluster.
+//   SSSP : the near/far label-correcting scheme of sssp.cu (bitmap sets,
+//          atomicMin, Delta buckets), scoped to the cluster.
 //   SSSP group : up to 32 SSSP queries on one graph as ONE multi-source
 //          traversal (msssp_core.cuh) scoped to the cluster, sharing every
 //          adjacency read; the host packs queries on the same graph into
@@ -155,41 +155,23 @@ __device__ void run_bfs(const Args &a, const Ctx &c, cg::cluster_group &cl, cons
 }
 
 // ---- SSSP -----------------------------------------------------------------
+// The bitmap near/far scheme of sssp.cu scoped to the cluster: near sets
+// N[2] and the far set are bitmaps, compacted into the binned lists once per
+// level, and a relaxation waits on no atomic.
 struct RelaxVisitor {
   const GraphDesc *g;
   uint32_t *dist, T;
-  uint32_t *inq_next, *farbm, *qnext, *farp, *farcount, qcap;
-  uint4 *cnext;
-  uint32_t ccap, huge;
-  Slot *nx;
-  uint32_t *err;
+  uint32_t *nnext, *farbm;
   unsigned long long visits;
   using aux_t = uint32_t;
   __device__ __forceinline__ uint32_t aux(uint32_t v) const { return __ldcg(dist + v); }
-  __device__ __forceinline__ void to_near(uint32_t v) {
-    const uint32_t w = v >> 5, bit = 1u << (v & 31u);
-    if (__ldcg(inq_next + w) & bit) return;
-    if (atomicOr(inq_next + w, bit) & bit) return;
-    const uint32_t b = __ldg(g->offs + v), e = __ldg(g->offs + v + 1);
-    if (!push_binned(v, b, e, huge, qnext, &nx->qcount, qcap, cnext, &nx->ccount, ccap))
-      atomicOr(err, kErrOverflow);
-  }
   __device__ __forceinline__ void edge(uint32_t, uint32_t du, uint32_t x) {
     ++visits;
     const uint32_t v = __ldg(g->cols + x);
     const uint32_t nd = du + __ldg(g->wts + x);
     if (nd >= __ldcg(dist + v)) return;
-    atomicMin(dist + v, nd);  // reduction; the bitmaps deduplicate the marks
-    if (nd < T) {
-      to_near(v);
-    } else {
-      const uint32_t w = v >> 5, bit = 1u << (v & 31u);
-      if (__ldcg(farbm + w) & bit) return;
-      if (atomicOr(farbm + w, bit) & bit) return;
-      const uint32_t pos = agg_reserve(farcount);
-      if (pos < qcap) farp[pos] = v;
-      else atomicOr(err, kErrOverflow);
-    }
+    atomicMin(dist + v, nd);  // reductions; a raced mark costs one redundant expansion
+    atomicOr((nd < T ? nnext : farbm) + (v >> 5), 1u << (v & 31u));
   }
 };
 
@@ -198,88 +180,95 @@ __device__ void run_sssp(const Args &a, const Ctx &c, cg::cluster_group &cl, con
                          WorkerCtl *ctl) {
   const uint32_t n = g->n, W = (n + 31) / 32;
   const uint64_t Wp = a.Wp;
-  uint32_t *inq[3] = {bm, bm + Wp, bm + 2 * Wp};
+  uint32_t *near[2] = {bm, bm + Wp};
   uint32_t *farbm = bm + 3 * Wp;
-  uint32_t *queue[2] = {lists, lists + a.cap};
-  uint32_t *far[2] = {lists + 2 * (uint64_t)a.cap, lists + 3 * (uint64_t)a.cap};
-  uint4 *ch[2] = {chunks, chunks + a.chunk_cap};
+  uint32_t *queue = lists;
   for (uint32_t i = c.ctid; i < n; i += c.cthreads) dist[i] = kBatchInfinit;
   for (uint32_t i = c.ctid; i < W; i += c.cthreads) {
-    inq[0][i] = 0u;
-    inq[1][i] = 0u;
-    inq[2][i] = 0u;
+    near[0][i] = 0u;
+    near[1][i] = 0u;
     farbm[i] = 0u;
   }
   if (c.ctid < 4 * sizeof(Slot) / 4) ((uint32_t *)ctl->slots)[c.ctid] = 0u;
   if (c.ctid < sizeof(FarCtl) / 4) ((uint32_t *)&ctl->far)[c.ctid] = 0u;
+  if (c.ctid == 0) {
+    ctl->far.minfar[0] = 0xFFFFFFFFu;
+    ctl->far.minfar[1] = 0xFFFFFFFFu;
+  }
   cl.sync();
   if (c.ctid == 0) {
     dist[src] = 0u;
-    const uint32_t b = __ldg(g->offs + src), e = __ldg(g->offs + src + 1);
-    if (!push_binned(src, b, e, a.huge, queue[0], &ctl->slots[0].qcount, a.cap, ch[0],
-                     &ctl->slots[0].ccount, a.chunk_cap))
-      atomicOr(&ctl->err, kErrOverflow);
+    near[0][src >> 5] = 1u << (src & 31u);
   }
   cl.sync();
-  uint32_t L = 0, T = a.delta, fsel = 0, splits = 0;
+  uint32_t L = 0, T = a.delta, splits = 0;
   unsigned long long visits = 0;
   while (true) {
-    Slot *cur = ctl->slots + (L & 3u), *nx = ctl->slots + ((L + 1) & 3u);
-    uint32_t *inq_next = inq[(L + 1) % 3], *inq_clr = inq[(L + 2) % 3];
-    for (uint32_t i = c.ctid; i < W; i += c.cthreads) inq_clr[i] = 0u;
+    Slot *sl = ctl->slots + (L & 3u);
     if (c.ctid < sizeof(Slot) / 4) ((uint32_t *)(ctl->slots + ((L + 2) & 3u)))[c.ctid] = 0u;
-    RelaxVisitor vis{g, dist, T, inq_next, farbm, queue[(L + 1) & 1u], far[fsel],
-                     &ctl->far.count[fsel], a.cap, ch[(L + 1) & 1u], a.chunk_cap, a.huge, nx,
-                     &ctl->err, 0ull};
-    expand_binned<kBatchBlock>(g->offs, queue[L & 1u], min(__ldcg(&cur->qcount), a.cap), ch[L & 1u],
-                               min(__ldcg(&cur->ccount), a.chunk_cap), vis, c.part, c.parts);
-    visits += vis.visits;
+    uint32_t *ncur = near[L & 1u], *nnext = near[(L + 1) & 1u];
+    bitmap_to_binned<kBatchBlock>(ncur, W, g->offs, a.huge, queue, &sl->qcount, a.cap, chunks,
+                                  &sl->ccount, a.chunk_cap, &ctl->err, c.part, c.parts);
     cl.sync();
-    ++L;
-    bool done = false;
-    while (__ldcg(&nx->qcount) + __ldcg(&nx->ccount) == 0) {
-      const uint32_t fc = min(__ldcg(&ctl->far.count[fsel]), a.cap);
-      if (fc == 0) {
-        done = true;
-        break;
-      }
+    const uint32_t qc = min(__ldcg(&sl->qcount), a.cap);
+    const uint32_t cc = min(__ldcg(&sl->ccount), a.chunk_cap);
+    if (qc + cc == 0) {
+      // nothing near: advance the threshold and split the far set into ncur
+      // (minfar[j & 1]: smallest distance left by split j - 1; FarCtl.count
+      // holds the split's moved / remaining counters)
       const uint32_t Told = T;
       uint32_t Tnew = T + a.delta;
       const uint32_t mf = __ldcg(&ctl->far.minfar[splits & 1u]);
-      if (splits && mf != 0xFFFFFFFFu && mf >= Tnew) Tnew = (mf / a.delta + 1) * a.delta;
-      if (c.ctid == 0) {
-        ctl->far.count[fsel ^ 1u] = 0u;
-        ctl->far.minfar[(splits + 1) & 1u] = 0xFFFFFFFFu;
+      if (mf != 0xFFFFFFFFu && mf >= Tnew) Tnew = (mf / a.delta + 1) * a.delta;
+      uint32_t moved = 0, remaining = 0, local_min = 0xFFFFFFFFu;
+      for (uint32_t w = c.ctid; w < W; w += c.cthreads) {
+        const uint32_t fw = __ldcg(farbm + w);
+        if (!fw) continue;
+        uint32_t keep = 0, mv = 0;
+        for (uint32_t bits = fw; bits; bits &= bits - 1) {
+          const uint32_t b = __ffs(bits) - 1;
+          const uint32_t d = __ldcg(dist + w * 32 + b);
+          if (d < Told) continue;
+          if (d < Tnew) {
+            mv |= 1u << b;
+          } else {
+            keep |= 1u << b;
+            local_min = min(local_min, d);
+          }
+        }
+        farbm[w] = keep;
+        if (mv) ncur[w] = mv;
+        moved += __popc(mv);
+        remaining += keep != 0;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        local_min = min(local_min, __shfl_down_sync(0xffffffffu, local_min, o));
+        moved += __shfl_down_sync(0xffffffffu, moved, o);
+        remaining += __shfl_down_sync(0xffffffffu, remaining, o);
+      }
+      if (lane_id() == 0) {
+        if (local_min != 0xFFFFFFFFu) atomicMin(&ctl->far.minfar[(splits + 1) & 1u], local_min);
+        if (moved) atomicAdd(&ctl->far.count[0], moved);
+        if (remaining) atomicAdd(&ctl->far.count[1], remaining);
       }
       cl.sync();
-      const uint32_t *fp = far[fsel];
-      uint32_t *kp = far[fsel ^ 1u];
-      uint32_t local_min = 0xFFFFFFFFu;
-      for (uint32_t i = c.ctid; i < fc; i += c.cthreads) {
-        const uint32_t v = __ldcg(fp + i);
-        const uint32_t d = __ldcg(dist + v);
-        const uint32_t w = v >> 5, bit = 1u << (v & 31u);
-        if (d < Told) {
-          atomicAnd(farbm + w, ~bit);
-        } else if (d < Tnew) {
-          atomicAnd(farbm + w, ~bit);
-          vis.to_near(v);
-        } else {
-          const uint32_t pos = agg_reserve(&ctl->far.count[fsel ^ 1u]);
-          kp[pos] = v;
-          local_min = min(local_min, d);
-        }
-      }
-      for (int o = 16; o > 0; o >>= 1)
-        local_min = min(local_min, __shfl_down_sync(0xffffffffu, local_min, o));
-      if (lane_id() == 0 && local_min != 0xFFFFFFFFu)
-        atomicMin(&ctl->far.minfar[(splits + 1) & 1u], local_min);
+      const uint32_t mv_all = __ldcg(&ctl->far.count[0]), rem_all = __ldcg(&ctl->far.count[1]);
+      if (c.ctid == 0) ctl->far.minfar[splits & 1u] = 0xFFFFFFFFu;
       T = Tnew;
-      fsel ^= 1u;
       ++splits;
       cl.sync();
+      if (c.ctid == 0) {
+        ctl->far.count[0] = 0u;
+        ctl->far.count[1] = 0u;
+      }
+      if (mv_all == 0 && rem_all == 0) break;
+      continue;
     }
-    if (done) break;
+    RelaxVisitor vis{g, dist, T, nnext, farbm, 0ull};
+    expand_binned<kBatchBlock>(g->offs, queue, qc, chunks, cc, vis, c.part, c.parts);
+    visits += vis.visits;
+    cl.sync();
+    ++L;
     if (L > 4u * n + 64u) {
       if (c.ctid == 0) atomicOr(&ctl->err, kErrLevels);
       break;
@@ -569,7 +558,7 @@ struct grus_batch {
   uint32_t ntasks = 0, nmembers = 0;   // of the staged plan
   grus::BatchState state;
   int cluster = 16, workers = 0;
-  uint32_t huge = 1024, delta = 96;
+  uint32_t huge = 1024, delta = 192;
   uint64_t max_n = 0, max_m = 0, total_out = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;

@@ -52,6 +52,63 @@ __device__ __forceinline__ bool push_binned(uint32_t v, uint32_t b, uint32_t e,
   return true;
 }
 
+// The set bits of bitmap `bm` (W words) become binned work lists as
+// push_binned would build them -- degree 1 .. huge-1 into the vertex queue,
+// degree >= huge into kChunk-edge chunks -- and every word is cleared as it
+// is read.  CTA `part` of `parts` owns a contiguous range of words and
+// reserves queue space once per 256 words (block scan of the counts).
+// Must be called by every thread of the CTA.
+template <int kBlock>
+__device__ __forceinline__ void bitmap_to_binned(uint32_t *bm, uint32_t W,
+                                                 const uint32_t *__restrict__ offs, uint32_t huge,
+                                                 uint32_t *q, uint32_t *qcount, uint32_t qcap,
+                                                 uint4 *c, uint32_t *ccount, uint32_t ccap,
+                                                 uint32_t *err, uint32_t part, uint32_t parts) {
+  __shared__ uint32_t s_base;
+  const uint32_t per = (W + parts - 1) / parts;
+  const uint32_t w0 = min(W, part * per), w1 = min(W, w0 + per);
+  for (uint32_t base = w0; base < w1; base += kBlock) {
+    const uint32_t w = base + threadIdx.x;
+    const uint32_t word = w < w1 ? __ldcg(bm + w) : 0u;
+    if (word) bm[w] = 0u;
+    uint32_t cnt = 0;
+    for (uint32_t bits = word; bits; bits &= bits - 1) {
+      const uint32_t v = w * 32 + (__ffs(bits) - 1);
+      const uint32_t b = __ldg(offs + v), e = __ldg(offs + v + 1);
+      const uint32_t d = e - b;
+      if (d == 0) continue;
+      if (d < huge) {
+        ++cnt;
+      } else {
+        const uint32_t nch = (d + kChunk - 1) / kChunk;
+        const uint32_t pos = atomicAdd(ccount, nch);
+        if (pos + nch > ccap) {
+          atomicOr(err, kErrOverflow);
+        } else {
+          for (uint32_t k = 0; k < nch; ++k)
+            c[pos + k] = make_uint4(v, b + k * kChunk, min(e, b + (k + 1) * kChunk), 0u);
+        }
+      }
+    }
+    uint32_t total = 0;
+    uint32_t at = block_exclusive_scan<kBlock>(cnt, &total);
+    if (threadIdx.x == 0 && total) s_base = atomicAdd(qcount, total);
+    __syncthreads();
+    if (cnt) {
+      at += s_base;
+      for (uint32_t bits = word; bits; bits &= bits - 1) {
+        const uint32_t v = w * 32 + (__ffs(bits) - 1);
+        const uint32_t d = __ldg(offs + v + 1) - __ldg(offs + v);
+        if (d == 0 || d >= huge) continue;
+        if (at < qcap) q[at] = v;
+        else atomicOr(err, kErrOverflow);
+        ++at;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // One tile: every thread of the CTA brings one source (v, [beg,end), aux);
 // an empty range means "no source".  CTA, warp and gather mappings in turn.
 // Must be called by every thread of the CTA.

@@ -175,56 +175,6 @@ struct RelaxVisitor {
   }
 };
 
-// Step 1: the set bits of `bm` become work: degree < huge into the vertex
-// queue (one reservation per CTA), degree >= huge into 1024-edge chunks.
-// Every word is cleared as it is read.  Each CTA owns a contiguous range of
-// words.
-__device__ __forceinline__ void bitmap_to_lists(const Args &a, uint32_t *bm, Slot *sl) {
-  __shared__ uint32_t s_base;
-  const uint32_t per = (a.W + gridDim.x - 1) / gridDim.x;
-  const uint32_t w0 = min(a.W, blockIdx.x * per), w1 = min(a.W, w0 + per);
-  for (uint32_t base = w0; base < w1; base += kBlock) {
-    const uint32_t w = base + threadIdx.x;
-    uint32_t word = w < w1 ? __ldcg(bm + w) : 0u;
-    if (word) bm[w] = 0u;
-    uint32_t cnt = 0;
-    for (uint32_t bits = word; bits; bits &= bits - 1) {
-      const uint32_t v = w * 32 + (__ffs(bits) - 1);
-      const uint32_t b = __ldg(a.offs + v), e = __ldg(a.offs + v + 1);
-      const uint32_t d = e - b;
-      if (d == 0) continue;
-      if (d < a.huge) {
-        ++cnt;
-      } else {
-        const uint32_t nch = (d + kChunk - 1) / kChunk;
-        const uint32_t pos = atomicAdd(&sl->ccount, nch);
-        if (pos + nch > a.chunk_cap) {
-          atomicOr(a.err, kErrOverflow);
-        } else {
-          for (uint32_t k = 0; k < nch; ++k)
-            a.chunks[pos + k] = make_uint4(v, b + k * kChunk, min(e, b + (k + 1) * kChunk), 0u);
-        }
-      }
-    }
-    uint32_t total = 0;
-    uint32_t at = block_exclusive_scan<kBlock>(cnt, &total);
-    if (threadIdx.x == 0 && total) s_base = atomicAdd(&sl->qcount, total);
-    __syncthreads();
-    if (cnt) {
-      at += s_base;
-      for (uint32_t bits = word; bits; bits &= bits - 1) {
-        const uint32_t v = w * 32 + (__ffs(bits) - 1);
-        const uint32_t d = __ldg(a.offs + v + 1) - __ldg(a.offs + v);
-        if (d == 0 || d >= a.huge) continue;
-        if (at < a.queue_cap) a.queue[at] = v;
-        else atomicOr(a.err, kErrOverflow);
-        ++at;
-      }
-    }
-    __syncthreads();
-  }
-}
-
 __global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
@@ -255,7 +205,8 @@ __global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
     Slot *sl = a.slots + (L & 3u);
     if (gtid < sizeof(Slot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[gtid] = 0u;
     uint32_t *ncur = a.near[L & 1u], *nnext = a.near[(L + 1) & 1u];
-    bitmap_to_lists(a, ncur, sl);
+    bitmap_to_binned<kBlock>(ncur, a.W, a.offs, a.huge, a.queue, &sl->qcount, a.queue_cap,
+                             a.chunks, &sl->ccount, a.chunk_cap, a.err, blockIdx.x, gridDim.x);
     if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
     const uint32_t qc = min(__ldcg(&sl->qcount), a.queue_cap);
     const uint32_t cc = min(__ldcg(&sl->ccount), a.chunk_cap);
@@ -282,7 +233,7 @@ __global__ void __launch_bounds__(kBlock) sssp_persistent(Args a) {
           }
         }
         a.farbm[w] = keep;
-        if (mv) ncur[w] = mv;  // ncur is all zero after bitmap_to_lists
+        if (mv) ncur[w] = mv;  // ncur is all zero after its compaction
         moved += __popc(mv);
         remaining += keep != 0;
       }
