@@ -215,6 +215,15 @@ def barrier(dist):
         dist.barrier()
 
 
+def host_threads():
+    """Every core this process may run on (torchrun sets OMP_NUM_THREADS=1 for
+    its workers; the CPU baselines ask for all cores explicitly)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
 def workload_spec(args):
     w = dict(WORKLOADS[args.workload])
     if args.scale:
@@ -432,7 +441,7 @@ def run_grus(args, dist, rank, local):
             if algo == "pagerank":
                 co, cc_, _ = g.copy_csc()
                 csc = oracle.CSR(co, cc_)
-            threads = oracle.omp_threads()
+            threads = host_threads()
             v, sample = cpu_run(w, csr, csc, src, srcs, threads)
             cpu = {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": sample}
@@ -480,7 +489,7 @@ def run_reference(args, dist, rank):
     srcs = None
     if algo in ("msbfs", "msssp"):
         srcs = msbfs_sources(g.n, lambda v: int(g.offs[v + 1]) - int(g.offs[v]), w["sources"], 4)
-    threads = oracle.omp_threads()
+    threads = host_threads()
     for _ in range(max(args.warmup - 1, 0)):
         cpu_run(w, g, csc, src, srcs, threads, budget_s=0.0, max_runs=1)
     rates = []
