@@ -13,8 +13,9 @@
 // Layout: in-edges (CSC) from grus_graph_build_csc; a contribution array
 // c(u) = r(u)/outdeg(u) double-buffered across iterations, so an iteration is
 // one fused pass: gather c over in-edges, form r, write c_next (and r on the
-// last iteration).  Per 256-vertex tile, in-degree is binned:
-//   >= kCtaTh (1024) : whole CTA strides the list, block reduction
+// last iteration).  In-degree is binned:
+//   >= kCtaTh (1024) : cut into 2048-edge pieces, one CTA per piece, the
+//                      piece sums added in order afterwards
 //   >= 32            : one warp, loads four wide, shuffle reduction
 //   <  32            : the warp's short lists laid end to end, one edge per
 //                      lane, segmented warp scan (every lane busy)
@@ -32,7 +33,8 @@ namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr uint32_t kCtaTh = 1024;
+constexpr uint32_t kCtaTh = 1024;   // in-degree from which a vertex is "heavy"
+constexpr uint32_t kHChunk = 2048;  // edges per heavy-vertex piece
 constexpr uint32_t kKahanTh = 16;
 
 struct Args {
@@ -44,6 +46,12 @@ struct Args {
   int iters;
   float *c[2];
   float *rank;
+  // heavy vertices (in-degree >= kCtaTh): heavy[i] = (v, first piece, pieces),
+  // pieces[j] = (v, begin, end, i), partial[j] = sum over piece j
+  uint4 *heavy, *pieces;
+  float *partial;
+  uint32_t heavy_cap, piece_cap;
+  uint32_t *hcount;  // [0] heavy vertices, [1] pieces
   GridBarrier *bar;
   uint32_t *err;
   uint64_t timeout_ns;
@@ -155,53 +163,58 @@ __device__ __forceinline__ float gather_short(const Args &a, const float *cs, ui
   return acc.value();
 }
 
+// One iteration is
+//   A. every warp, independently, takes groups of 32 consecutive vertices:
+//      in-lists of 32..kCtaTh-1 edges by the whole warp (four loads in
+//      flight), shorter ones laid end to end (gather_short); heavy vertices
+//      are skipped;
+//   B. every CTA takes pieces of kHChunk edges of the heavy vertices and
+//      writes each piece's sum;
+//   -- grid barrier --
+//   C. each heavy vertex adds its pieces in order (compensated) and finishes;
+//   -- grid barrier --
+// so no block barrier separates the warps of a light tile, and a heavy
+// vertex is spread over many CTAs.  The heavy lists are built once per call.
 __global__ void __launch_bounds__(kBlock) pr_persistent(Args a) {
-  __shared__ uint32_t s_owner, s_v, s_beg, s_end;
   __shared__ float s_part[kBlock / 32];
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
   const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  const uint32_t gwarp = gtid >> 5, nwarps = nthreads >> 5;
   const float r0 = 1.0f / (float)a.n;
-  for (uint32_t v = gtid; v < a.n; v += nthreads) a.c[0][v] = r0 * outdeg_inv(a, v);
+  for (uint32_t v = gtid; v < a.n; v += nthreads) {
+    a.c[0][v] = r0 * outdeg_inv(a, v);
+    const uint32_t b = __ldg(a.toffs + v), e = __ldg(a.toffs + v + 1);
+    if (e - b >= kCtaTh) {
+      const uint32_t np = (e - b + kHChunk - 1) / kHChunk;
+      const uint32_t hi = atomicAdd(&a.hcount[0], 1u);
+      const uint32_t p0 = atomicAdd(&a.hcount[1], np);
+      if (hi >= a.heavy_cap || p0 + np > a.piece_cap) {
+        atomicOr(a.err, kErrOverflow);
+        continue;
+      }
+      a.heavy[hi] = make_uint4(v, p0, np, 0u);
+      for (uint32_t k = 0; k < np; ++k)
+        a.pieces[p0 + k] = make_uint4(v, b + k * kHChunk, min(e, b + (k + 1) * kHChunk), hi);
+    }
+  }
   if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+  const uint32_t nheavy = min(__ldcg(&a.hcount[0]), a.heavy_cap);
+  const uint32_t npieces = min(__ldcg(&a.hcount[1]), a.piece_cap);
 
   for (int it = 0; it < a.iters; ++it) {
     const float *cs = a.c[it & 1];
     float *cn = a.c[(it + 1) & 1];
     const bool last = it + 1 == a.iters;
-    for (uint32_t base = blockIdx.x * kBlock; base < a.n; base += gridDim.x * kBlock) {
-      const uint32_t v = base + threadIdx.x;
+    // A: light vertices, warp by warp
+    for (uint32_t g0 = gwarp * 32; g0 < a.n; g0 += nwarps * 32) {
+      const uint32_t v = g0 + lane;
       uint32_t beg = 0, end = 0;
       if (v < a.n) {
         beg = __ldg(a.toffs + v);
         end = __ldg(a.toffs + v + 1);
       }
-      bool done = v >= a.n;
-      // CTA-cooperative for very high in-degree (one block vote per tile
-      // when no vertex qualifies)
-      while (__syncthreads_or(!done && end - beg >= kCtaTh)) {
-        if (!done && end - beg >= kCtaTh) s_owner = threadIdx.x;  // any qualifying thread wins
-        __syncthreads();
-        const uint32_t owner = s_owner;
-        if (threadIdx.x == owner) {
-          s_v = v;
-          s_beg = beg;
-          s_end = end;
-          done = true;
-        }
-        __syncthreads();
-        const uint32_t cv = s_v, cb = s_beg, ce = s_end;
-        float part = warp_sum(gather_seq(a, cs, cb + threadIdx.x, ce, kBlock));
-        if (lane == 0) s_part[warp] = part;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-          float tot = 0.f;
-          for (int i = 0; i < kBlock / 32; ++i) tot += s_part[i];
-          finish(a, cv, tot, cn, last);
-        }
-        __syncthreads();
-      }
-      // warp-cooperative
+      bool done = v >= a.n || end - beg >= kCtaTh;
       while (true) {
         const uint32_t ball = __ballot_sync(0xffffffffu, !done && end - beg >= 32);
         if (!ball) break;
@@ -213,9 +226,29 @@ __global__ void __launch_bounds__(kBlock) pr_persistent(Args a) {
         const float tot = warp_sum(gather_seq(a, cs, wb + lane, we, 32));
         if ((int)lane == leader) finish(a, wv, tot, cn, last);
       }
-      // the warp's short lists, end to end
-      const float s = gather_short(a, cs, beg, done ? 0u : end - beg);
-      if (!done) finish(a, v, s, cn, last);
+      const float sum = gather_short(a, cs, beg, done ? 0u : end - beg);
+      if (!done) finish(a, v, sum, cn, last);
+    }
+    // B: pieces of heavy vertices, CTA by CTA
+    for (uint32_t p = blockIdx.x; p < npieces; p += gridDim.x) {
+      const uint4 pc = __ldcg(a.pieces + p);
+      const float part = warp_sum(gather_seq(a, cs, pc.y + threadIdx.x, pc.z, kBlock));
+      if (lane == 0) s_part[warp] = part;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        float tot = 0.f;
+        for (int i = 0; i < kBlock / 32; ++i) tot += s_part[i];
+        a.partial[p] = tot;
+      }
+      __syncthreads();
+    }
+    if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+    // C: heavy vertices add their pieces in order
+    for (uint32_t h = gtid; h < nheavy; h += nthreads) {
+      const uint4 hv = __ldcg(a.heavy + h);
+      KSum k;
+      for (uint32_t j = 0; j < hv.z; ++j) k.add(__ldcg(a.partial + hv.y + j));
+      finish(a, hv.x, k.value(), cn, last);
     }
     if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
   }
@@ -224,17 +257,23 @@ __global__ void __launch_bounds__(kBlock) pr_persistent(Args a) {
 struct Workspace {
   float *c = nullptr;   // 2 * n contributions
   float *rank = nullptr;
+  uint4 *heavy = nullptr, *pieces = nullptr;
+  float *partial = nullptr;
+  uint32_t heavy_cap = 0, piece_cap = 0;
   char *ctrl = nullptr, *ctrl_host = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
-constexpr size_t kOffBar = 0, kOffErr = 64, kCtrlBytes = 128;
+constexpr size_t kOffBar = 0, kOffErr = 64, kOffHeavy = 96, kCtrlBytes = 128;
 
 void ws_free(void *p) {
   Workspace *w = (Workspace *)p;
   if (!w) return;
   cudaFree(w->c);
   cudaFree(w->rank);
+  cudaFree(w->heavy);
+  cudaFree(w->pieces);
+  cudaFree(w->partial);
   cudaFree(w->ctrl);
   if (w->ctrl_host) cudaFreeHost(w->ctrl_host);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -249,7 +288,12 @@ int ws_get(grus_graph *g, Workspace **out) {
   }
   Workspace *w = new Workspace();
   const uint64_t n1 = std::max<uint64_t>(g->n, 1);
+  w->heavy_cap = (uint32_t)std::min<uint64_t>(n1, g->m / kCtaTh + 1);
+  w->piece_cap = (uint32_t)(g->m / kHChunk + w->heavy_cap + 1);
   cudaError_t e = cudaMalloc(&w->c, 2 * n1 * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&w->heavy, (size_t)w->heavy_cap * sizeof(uint4));
+  if (e == cudaSuccess) e = cudaMalloc(&w->pieces, (size_t)w->piece_cap * sizeof(uint4));
+  if (e == cudaSuccess) e = cudaMalloc(&w->partial, (size_t)w->piece_cap * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
   if (e == cudaSuccess) e = cudaMemset(w->ctrl, 0, kCtrlBytes);
   if (e == cudaSuccess) e = cudaMallocHost(&w->ctrl_host, kCtrlBytes);
@@ -300,6 +344,12 @@ extern "C" int grus_pagerank(grus_graph *g, float damping, int iters, float *ran
   a.c[0] = w->c;
   a.c[1] = w->c + g->n;
   a.rank = dev_out ? rank : w->rank;
+  a.heavy = w->heavy;
+  a.pieces = w->pieces;
+  a.partial = w->partial;
+  a.heavy_cap = w->heavy_cap;
+  a.piece_cap = w->piece_cap;
+  a.hcount = (uint32_t *)(w->ctrl + kOffHeavy);
   a.bar = (GridBarrier *)(w->ctrl + kOffBar);
   a.err = (uint32_t *)(w->ctrl + kOffErr);
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
@@ -310,6 +360,7 @@ extern "C" int grus_pagerank(grus_graph *g, float damping, int iters, float *ran
     GRUS_CUDA_TRY(cudaStreamSynchronize(s));
     return GRUS_OK;
   }
+  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffHeavy, 0, 8, s));  // heavy-list counters
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
   void *args[] = {&a};
   rc = launch_persistent((const void *)pr_persistent, args, kBlock, (int)g->tuning.ctas_per_sm,
