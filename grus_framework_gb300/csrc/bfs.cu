@@ -747,3 +747,17 @@ extern "C" int grus_bfs_static(uint64_t n, uint64_t m, const uint32_t *offsets,
   stats->edges_reached = sm->mr;
   return GRUS_OK;
 }
+
+namespace grus {
+CtrlView bfs_ctrl(grus_graph *g) {
+  CtrlView v;
+  std::lock_guard<std::mutex> lk(g->mu);
+  const Workspace *w = (const Workspace *)g->ws[kWsBfs];
+  if (w) {
+    v.ctrl = w->ctrl;
+    v.bytes = kCtrlBytes;
+    v.err_off = kOffErr;
+  }
+  return v;
+}
+}  // namespace grus

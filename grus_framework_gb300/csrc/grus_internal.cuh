@@ -87,4 +87,16 @@ int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
 int msssp_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
               grus_stats *stats, cudaStream_t s);
 
+// Device control block of a graph's workspace for one algorithm (ctrl null
+// before the algorithm's first call on the graph), for callers that launch
+// without waiting and check the launch's error word later.
+struct CtrlView {
+  char *ctrl = nullptr;
+  size_t bytes = 0, err_off = 0;
+};
+CtrlView bfs_ctrl(grus_graph *g);
+CtrlView sssp_ctrl(grus_graph *g);
+CtrlView msbfs_ctrl(grus_graph *g);
+CtrlView msssp_ctrl(grus_graph *g);
+
 }  // namespace grus

@@ -483,3 +483,17 @@ extern "C" int grus_bfs_multi(grus_graph *g, const uint32_t *srcs, int k, uint32
   }
   return GRUS_OK;
 }
+
+namespace grus {
+CtrlView msbfs_ctrl(grus_graph *g) {
+  CtrlView v;
+  std::lock_guard<std::mutex> lk(g->mu);
+  const Workspace *w = (const Workspace *)g->ws[kWsMsBfs];
+  if (w) {
+    v.ctrl = w->ctrl;
+    v.bytes = kCtrlBytes;
+    v.err_off = kOffErr;
+  }
+  return v;
+}
+}  // namespace grus

@@ -18,7 +18,7 @@ namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr uint32_t kDefDelta = 96;
+constexpr uint32_t kDefDelta = 384;
 constexpr int kMaxSources = 32;
 using ms::kPiece;
 using ms::Slot;
@@ -253,3 +253,17 @@ extern "C" int grus_sssp_multi(grus_graph *g, const uint32_t *srcs, int k, uint3
   if (tmp) cudaFree(tmp);
   return rc;
 }
+
+namespace grus {
+CtrlView msssp_ctrl(grus_graph *g) {
+  CtrlView v;
+  std::lock_guard<std::mutex> lk(g->mu);
+  const Workspace *w = (const Workspace *)g->ws[kWsMsSssp];
+  if (w) {
+    v.ctrl = w->ctrl;
+    v.bytes = kCtrlBytes;
+    v.err_off = kOffErr;
+  }
+  return v;
+}
+}  // namespace grus

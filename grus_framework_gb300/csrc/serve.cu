@@ -12,13 +12,15 @@
 //   Big graphs (at least big_edges edges): one cluster would take many times
 //     longer than the whole GPU, so a second thread runs the whole-GPU
 //     persistent kernels (grus_bfs / grus_sssp) one launch at a time, and
-//     packs the queued requests of one algorithm on the same graph -- up to
-//     64 BFS (msbfs.cu) or 32 SSSP (msssp.cu) -- into one multi-source launch
-//     that writes each request's own output.
+//     packs the queued SSSP requests on the same graph -- up to 32 -- into one
+//     multi-source launch (msssp.cu) that writes each request's own output;
+//     BFS requests run as single direction-optimising launches.
 //     A graph's workspace is allocated only if free HBM covers it plus the
-//     reserve.
-// Completion is observed with an event per slot (small lane) or when the
-// whole-GPU call returns (big lane); latency is completion time minus
+//     reserve.  Up to four launches are queued on the lane's stream; each
+//     copies its error word to pinned memory and records an event, so the
+//     lane never waits on the host between queries.
+// Completion is observed with an event per slot (small lane) or per queued
+// launch (big lane); latency is completion time minus
 // submission time on the host clock.
 // The reference has no serving path (one query per process run).
 #include <algorithm>
@@ -239,71 +241,146 @@ void complete(grus_server *s, const Request &r, int status, Clock::time_point no
   ++s->finished;
 }
 
+// One whole-GPU launch of the big lane, in flight on the lane's stream.
+struct BigJob {
+  std::vector<Request> group;
+  cudaEvent_t done = nullptr;
+  uint32_t *h_err = nullptr;  // pinned copy of the launch's error word
+  CtrlView ctrl;
+};
+
+// Launches one group without waiting: the kernel, a copy of its error word
+// into pinned memory and a reset of that word, then an event.  Launches
+// queue back to back on the lane's stream, so the GPU runs them without the
+// host round trip between queries.
+int big_launch(grus_server *s, BigJob &j) {
+  const Request &r = j.group[0];
+  grus_graph *g = s->graphs[r.graph];
+  const bool multi = j.group.size() > 1;
+  if (!big_workspace_ready(g, r.algo, multi)) {
+    size_t free_b = 0, total_b = 0;
+    GRUS_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    if (free_b < big_workspace_bytes(g, r.algo, multi) + s->reserve) return GRUS_ENOMEM;
+  }
+  int rc;
+  if (!multi) {
+    rc = r.algo == GRUS_ALGO_SSSP ? grus_sssp(g, r.src, r.out, nullptr, s->big_stream)
+                                  : grus_bfs(g, r.src, r.out, nullptr, s->big_stream);
+  } else {
+    uint32_t srcs[64];
+    uint32_t *outs[64];
+    for (size_t i = 0; i < j.group.size(); ++i) {
+      srcs[i] = j.group[i].src;
+      outs[i] = j.group[i].out;
+    }
+    rc = r.algo == GRUS_ALGO_SSSP
+             ? msssp_run(g, srcs, (int)j.group.size(), outs, nullptr, s->big_stream)
+             : msbfs_run(g, srcs, (int)j.group.size(), outs, nullptr, s->big_stream);
+  }
+  if (rc) return rc;
+  j.ctrl = r.algo == GRUS_ALGO_SSSP ? (multi ? msssp_ctrl(g) : sssp_ctrl(g))
+                                    : (multi ? msbfs_ctrl(g) : bfs_ctrl(g));
+  *j.h_err = 0;
+  if (j.ctrl.ctrl) {
+    GRUS_CUDA_TRY(cudaMemcpyAsync(j.h_err, j.ctrl.ctrl + j.ctrl.err_off, 4, cudaMemcpyDeviceToHost,
+                                  s->big_stream));
+    GRUS_CUDA_TRY(cudaMemsetAsync(j.ctrl.ctrl + j.ctrl.err_off, 0, 4, s->big_stream));
+  }
+  GRUS_CUDA_TRY(cudaEventRecord(j.done, s->big_stream));
+  return GRUS_OK;
+}
+
+void big_finish(grus_server *s, std::vector<Request> &group, int rc) {
+  const auto now = Clock::now();
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (rc == GRUS_ENOMEM) {
+    s->rejected += group.size();
+  } else {
+    ++s->big_launches;
+    s->big_queries += group.size();
+    s->admitted += group.size();
+  }
+  for (const Request &q : group) complete(s, q, rc, now);
+  s->cv.notify_all();
+}
+
 void big_scheduler(grus_server *s) {
   cudaSetDevice(s->device);
-  std::vector<Request> group;
-  group.reserve(64);
-  while (true) {
-    group.clear();
-    {
-      std::unique_lock<std::mutex> lk(s->mu);
-      s->cv.wait_for(lk, std::chrono::milliseconds(50),
-                     [&] { return s->stop.load() || !s->big_pending.empty(); });
-      if (s->stop.load()) return;
-      if (s->big_pending.empty()) continue;
-      const Request first = s->big_pending.front();
-      s->big_pending.pop_front();
-      group.push_back(first);
+  constexpr int kDepth = 4;  // launches queued on the lane's stream
+  std::vector<BigJob> jobs(kDepth);
+  for (BigJob &j : jobs) {
+    cudaEventCreateWithFlags(&j.done, cudaEventDisableTiming);
+    cudaMallocHost(&j.h_err, 4);
+    j.group.reserve(64);
+  }
+  std::deque<int> inflight, spare;
+  for (int i = 0; i < kDepth; ++i) spare.push_back(i);
+  while (!s->stop.load()) {
+    bool progress = false;
+    // completions, in launch order
+    while (!inflight.empty()) {
+      BigJob &j = jobs[inflight.front()];
+      const cudaError_t q = cudaEventQuery(j.done);
+      if (q == cudaErrorNotReady) break;
+      int rc = q == cudaSuccess ? GRUS_OK : status_from_cuda(q);
+      if (rc == GRUS_OK && *j.h_err) {
+        rc = status_from_device_error(*j.h_err);
+        // the failed launch may have left its barrier state behind: drain the
+        // lane and clear the control block before the next launch on it
+        cudaStreamSynchronize(s->big_stream);
+        if (j.ctrl.ctrl) cudaMemset(j.ctrl.ctrl, 0, j.ctrl.bytes);
+      }
+      big_finish(s, j.group, rc);
+      spare.push_back(inflight.front());
+      inflight.pop_front();
+      progress = true;
+    }
+    // launches
+    while (!spare.empty()) {
+      BigJob &j = jobs[spare.front()];
+      j.group.clear();
       {
-        const size_t cap = first.algo == GRUS_ALGO_BFS ? 64 : 32;
-        for (auto it = s->big_pending.begin(); it != s->big_pending.end() && group.size() < cap;) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->big_pending.empty()) break;
+        const Request first = s->big_pending.front();
+        s->big_pending.pop_front();
+        j.group.push_back(first);
+        // SSSP requests on one graph share a multi-source launch (it
+        // amortises the adjacency reads over up to 32 sources); BFS requests
+        // run alone: one direction-optimising BFS skips most edges, and a
+        // 64-source pack on a small or isolated-source query costs more than
+        // the single launches it replaces
+        const size_t cap = first.algo == GRUS_ALGO_BFS ? 1 : 32;
+        for (auto it = s->big_pending.begin(); it != s->big_pending.end() && j.group.size() < cap;) {
           if (it->graph == first.graph && it->algo == first.algo) {
-            group.push_back(*it);
+            j.group.push_back(*it);
             it = s->big_pending.erase(it);
           } else {
             ++it;
           }
         }
       }
-    }
-    const Request &r = group[0];
-    grus_graph *g = s->graphs[r.graph];
-    const bool multi = group.size() > 1;
-    int rc = GRUS_OK;
-    if (!big_workspace_ready(g, r.algo, multi)) {
-      size_t free_b = 0, total_b = 0;
-      const cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
-      if (e != cudaSuccess) rc = status_from_cuda(e);
-      else if (free_b < big_workspace_bytes(g, r.algo, multi) + s->reserve) rc = GRUS_ENOMEM;
-    }
-    if (rc == GRUS_OK) {
-      grus_stats st;  // a stats call waits for the launch and checks its error word
-      if (!multi) {
-        rc = r.algo == GRUS_ALGO_SSSP ? grus_sssp(g, r.src, r.out, &st, s->big_stream)
-                                      : grus_bfs(g, r.src, r.out, &st, s->big_stream);
-      } else {
-        uint32_t srcs[64];
-        uint32_t *outs[64];
-        for (size_t i = 0; i < group.size(); ++i) {
-          srcs[i] = group[i].src;
-          outs[i] = group[i].out;
-        }
-        rc = r.algo == GRUS_ALGO_SSSP
-                 ? msssp_run(g, srcs, (int)group.size(), outs, &st, s->big_stream)
-                 : msbfs_run(g, srcs, (int)group.size(), outs, &st, s->big_stream);
+      progress = true;
+      const int rc = big_launch(s, j);
+      if (rc) {
+        big_finish(s, j.group, rc);
+        continue;
       }
+      inflight.push_back(spare.front());
+      spare.pop_front();
     }
-    const auto now = Clock::now();
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (rc == GRUS_ENOMEM) {
-      s->rejected += group.size();
-    } else {
-      ++s->big_launches;
-      s->big_queries += group.size();
-      s->admitted += group.size();
-    }
-    for (const Request &q : group) complete(s, q, rc, now);
-    s->cv.notify_all();
+    if (progress) continue;
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (inflight.empty())
+      s->cv.wait_for(lk, std::chrono::milliseconds(50),
+                     [&] { return s->stop.load() || !s->big_pending.empty(); });
+    else
+      s->cv.wait_for(lk, std::chrono::microseconds(20));
+  }
+  cudaStreamSynchronize(s->big_stream);
+  for (BigJob &j : jobs) {
+    cudaEventDestroy(j.done);
+    cudaFreeHost(j.h_err);
   }
 }
 
@@ -364,7 +441,14 @@ int grus_server_create(grus_graph *const *graphs, int ngraphs, const grus_server
     set_last_error(cudaGetErrorString(e));
     return status_from_cuda(e);
   }
-  e = cudaStreamCreateWithFlags(&s->big_stream, cudaStreamNonBlocking);
+  // The big lane's persistent launches need all their CTAs resident at once
+  // while the small lane keeps launching cluster workers on other streams:
+  // at the highest stream priority their pending CTAs take freed SM
+  // resources before new small-lane work does, so a grid barrier is never
+  // left waiting behind a stream of small launches.
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  e = cudaStreamCreateWithPriority(&s->big_stream, cudaStreamNonBlocking, prio_greatest);
   if (e != cudaSuccess) {
     cudaFree(s->d_graphs);
     delete s;

@@ -404,3 +404,17 @@ extern "C" int grus_sssp_trace(grus_graph *g, grus_level_trace *out, int max_lev
   }
   return levels;
 }
+
+namespace grus {
+CtrlView sssp_ctrl(grus_graph *g) {
+  CtrlView v;
+  std::lock_guard<std::mutex> lk(g->mu);
+  const Workspace *w = (const Workspace *)g->ws[kWsSssp];
+  if (w) {
+    v.ctrl = w->ctrl;
+    v.bytes = kCtrlBytes;
+    v.err_off = kOffErr;
+  }
+  return v;
+}
+}  // namespace grus

@@ -295,9 +295,9 @@ GRUS_API int grus_batch_free(grus_batch *b);
  * of the batch engine with its own device state and stream) as soon as a slot
  * is free, allocating a slot's state only if free HBM covers it plus
  * hbm_reserve_bytes; admitted queries overlap on the device.  Big graphs: a
- * second thread runs whole-GPU persistent launches one at a time, and packs
- * the queued queries of one algorithm on the same graph (up to 64 BFS or 32
- * SSSP) into one multi-source launch; a graph's workspace is allocated only if free HBM covers it plus
+ * second thread queues whole-GPU persistent launches back to back on a
+ * high-priority stream, and packs the queued SSSP queries on the same graph
+ * (up to 32) into one multi-source launch; a graph's workspace is allocated only if free HBM covers it plus
  * the reserve.  Latency is measured from submit to observed completion on the
  * host clock. */
 typedef struct grus_server grus_server;
@@ -322,8 +322,8 @@ typedef struct grus_server_stats {
   uint64_t submitted, admitted, completed, pending, rejected;
   uint32_t slots, slots_ready;
   uint64_t big_launches;     /* whole-GPU launches of the big-graph lane */
-  uint64_t big_queries;      /* queries they served (queries of one algorithm
-                                on one graph share a multi-source launch) */
+  uint64_t big_queries;      /* queries they served (SSSP queries on one graph
+                                share a multi-source launch) */
 } grus_server_stats;
 
 GRUS_API int grus_server_create(grus_graph *const *graphs, int ngraphs,

@@ -69,15 +69,15 @@ def test_server_rejects_bad_submissions(grus, graphs):
 
 def test_server_big_lane_groups_bfs_and_matches_alone(grus, graphs):
     """With big_edges=1 every graph is served by the whole-GPU lane: queued
-    queries of one algorithm on one graph share multi-source launches, and
-    each result equals the query run alone."""
+    SSSP queries on one graph share multi-source launches, BFS queries run
+    alone, and each result equals the query run alone."""
     torch = pytest.importorskip("torch")
     srv = grus.Server(graphs, slots=2, big_edges=1)
     rng = np.random.default_rng(7)
     reqs, outs = [], []
     for tag in range(150):
         gi = int(rng.integers(len(graphs)))
-        algo = grus.ALGO_BFS if tag % 5 else grus.ALGO_SSSP
+        algo = grus.ALGO_SSSP if tag % 5 else grus.ALGO_BFS
         src = int(rng.integers(graphs[gi].n))
         out = torch.empty(graphs[gi].n, dtype=torch.int32, device="cuda")
         reqs.append((gi, algo, src))
