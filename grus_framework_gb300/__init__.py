@@ -121,6 +121,7 @@ def _load():
         "grus_strerror": ([i32], C.c_char_p),
         "grus_last_error": ([], C.c_char_p),
         "grus_device_init": ([i32], i32),
+        "grus_check_wait_limit": ([C.c_uint32], i32),
         "grus_graph_from_csr": ([u64, u64, vp, vp, vp, u32, i32, u64, PG], i32),
         "grus_graph_load_gr": ([C.c_char_p, i32, i32, u64, PG], i32),
         "grus_graph_save_gr": ([vp, C.c_char_p], i32),
@@ -180,6 +181,12 @@ def _strerror(status):
 def _check(status, what):
     if status != 0:
         raise GrusError(status, what, lib.grus_last_error().decode())
+
+
+def check_wait_limit(timeout_ms: int = 100) -> int:
+    """Runs the bounded-wait diagnostic (include/grus.h grus_check_wait_limit);
+    returns its status code (ETIMEDOUT when the wait ended by its limit)."""
+    return lib.grus_check_wait_limit(timeout_ms)
 
 
 def version() -> str:

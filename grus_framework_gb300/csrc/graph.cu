@@ -167,6 +167,12 @@ __global__ void k_max_degree(const uint32_t *__restrict__ offs, uint64_t n,
   if ((threadIdx.x & 31) == 0) atomicMax(best, local);
 }
 
+// One CTA enters the persistent kernels' grid barrier; the host presets its
+// arrival count so the episode cannot complete and the wait must time out.
+__global__ void k_wait_limit(GridBarrier *bar, uint32_t *err, uint64_t timeout_ns) {
+  grid_sync(bar, err, timeout_ns);
+}
+
 static int grid_for(uint64_t work, int block = 256) {
   const int sms = std::max(device_sm_count(), 1);
   const uint64_t want = (work + block - 1) / block;
@@ -444,6 +450,36 @@ int grus_device_init(int device) {
   GRUS_CUDA_TRY(cudaSetDevice(device));
   GRUS_CUDA_TRY(cudaFree(nullptr));
   return GRUS_OK;
+}
+
+int grus_check_wait_limit(uint32_t timeout_ms) {
+  if (timeout_ms < 1 || timeout_ms > 10000) return GRUS_EINVAL;
+  char *ctrl = nullptr;
+  GRUS_CUDA_TRY(cudaMalloc(&ctrl, 64));
+  // barrier at offset 0, error word at 32; one arrival already counted, so
+  // the single CTA of the launch never sees the episode complete
+  GridBarrier preset{1u, 0u, 0u, 0u};
+  cudaError_t e = cudaMemset(ctrl, 0, 64);
+  if (e == cudaSuccess) e = cudaMemcpy(ctrl, &preset, sizeof(preset), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_wait_limit<<<1, 32>>>((GridBarrier *)ctrl, (uint32_t *)(ctrl + 32),
+                            (uint64_t)timeout_ms * 1000000ull);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  uint32_t err = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&err, ctrl + 32, 4, cudaMemcpyDeviceToHost);
+  cudaFree(ctrl);
+  if (e != cudaSuccess) {
+    set_last_error(cudaGetErrorString(e));
+    return status_from_cuda(e);
+  }
+  if (err & kErrTimeout) {
+    set_last_error("device wait ended at its time limit (as intended by this check)");
+    return GRUS_ETIMEDOUT;
+  }
+  set_last_error("device wait did not report its time limit");
+  return GRUS_ECUDA;
 }
 
 int grus_graph_from_csr(uint64_t n, uint64_t m, const uint32_t *offsets,

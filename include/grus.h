@@ -119,6 +119,13 @@ GRUS_API const char *grus_strerror(int status);
 GRUS_API const char *grus_last_error(void);
 /* Select and initialise a device (FLAGS_device, include/app.cuh:18). */
 GRUS_API int grus_device_init(int device);
+/* Diagnostic of the bounded device waits, no counterpart in the reference
+ * (whose kernels never wait on one another): runs the grid barrier of the
+ * persistent kernels in a one-CTA launch whose barrier can never complete
+ * (its arrival count is preset), so the wait must end by its time limit.
+ * Returns GRUS_ETIMEDOUT after about timeout_ms (1..10000) with the device
+ * context still usable, or another status if the wait did not behave. */
+GRUS_API int grus_check_wait_limit(uint32_t timeout_ms);
 
 /* ---- graphs -------------------------------------------------------------- */
 /* CSR from host arrays.  Replaces graph_t<CSR> filled by
