@@ -309,8 +309,23 @@ void big_scheduler(grus_server *s) {
   constexpr int kDepth = 4;  // launches queued on the lane's stream
   std::vector<BigJob> jobs(kDepth);
   for (BigJob &j : jobs) {
-    cudaEventCreateWithFlags(&j.done, cudaEventDisableTiming);
-    cudaMallocHost(&j.h_err, 4);
+    cudaError_t e = cudaEventCreateWithFlags(&j.done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMallocHost(&j.h_err, 4);
+    if (e != cudaSuccess) {
+      // no lane state: fail every big-graph request from now on
+      cudaGetLastError();
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->error = status_from_cuda(e);
+      set_last_error(std::string("server big lane: ") + cudaGetErrorString(e));
+      for (const Request &q : s->big_pending) complete(s, q, s->error, Clock::now());
+      s->big_pending.clear();
+      s->cv.notify_all();
+      for (BigJob &k : jobs) {
+        if (k.done) cudaEventDestroy(k.done);
+        if (k.h_err) cudaFreeHost(k.h_err);
+      }
+      return;
+    }
     j.group.reserve(64);
   }
   std::deque<int> inflight, spare;
