@@ -16,6 +16,10 @@
 //          traversal (msssp_core.cuh) scoped to the cluster, sharing every
 //          adjacency read; the host packs queries on the same graph into
 //          such groups.
+// Queries on graphs of at least big_edges edges do not go to the cluster
+// workers: a 16-CTA worker is a small slice of the GPU and such a query would
+// set the batch's critical path, so they run first as whole-GPU launches
+// (SSSP packed up to 32 sources per multi-source launch).
 // Results are bit-exact against single-query runs (BFS depths and SSSP
 // distances are schedule-independent).  The same kernel, launched with one
 // worker on a stream, is the unit of work of the query server (serve.cu).
@@ -556,6 +560,10 @@ struct grus_batch {
   uint32_t member_cap = 0;
   uint32_t group = 1;                  // SSSP queries per multi-source group
   uint32_t ntasks = 0, nmembers = 0;   // of the staged plan
+  uint64_t big_edges = 1ull << 23;     // graphs served by whole-GPU launches
+  std::vector<uint8_t> big;            // per graph
+  uint32_t *h_errs = nullptr;          // pinned error words of whole-GPU launches
+  uint32_t err_cap = 0;
   grus::BatchState state;
   int cluster = 16, workers = 0;
   uint32_t huge = 1024, delta = 192;
@@ -580,12 +588,16 @@ int grus_batch_create(grus_graph *const *graphs, int ngraphs, const grus_batch_c
   grus_batch *b = new grus_batch();
   b->graphs.assign(graphs, graphs + ngraphs);
   std::vector<GraphDesc> descs;
+  if (cfg && cfg->big_edges) b->big_edges = cfg->big_edges == 0xFFFFFFFFu ? ~0ull : cfg->big_edges;
   for (int i = 0; i < ngraphs; ++i) {
     if (!graphs[i]) {
       delete b;
       return GRUS_EINVAL;
     }
     descs.push_back(describe(graphs[i]));
+    const bool big = graphs[i]->m >= b->big_edges;
+    b->big.push_back(big ? 1 : 0);
+    if (big) continue;  // the cluster workers never see this graph
     b->max_n = std::max<uint64_t>(b->max_n, graphs[i]->n);
     b->max_m = std::max<uint64_t>(b->max_m, graphs[i]->m);
   }
@@ -663,6 +675,7 @@ static int ensure_members(grus_batch *b, uint32_t n) {
   drop_graph(b);
   cudaFree(b->d_msrc);
   cudaFree(b->d_moff);
+  if (b->h_errs) cudaFreeHost(b->h_errs);
   cudaFreeHost(b->h_msrc);
   cudaFreeHost(b->h_moff);
   b->d_msrc = b->h_msrc = nullptr;
@@ -784,12 +797,88 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
   cudaStream_t s = (cudaStream_t)stream;
   // the pinned staging buffers are read by the previous run's copies: wait
   if (b->in_flight) GRUS_CUDA_TRY(cudaEventSynchronize(b->done));
-  int rc = stage_tasks(b, queries, nq);
-  if (rc) return rc;
+  std::vector<grus_query> small_q;
+  std::vector<int> big_q;
+  small_q.reserve(nq);
+  for (int i = 0; i < nq; ++i) {
+    if (b->big[queries[i].graph]) big_q.push_back(i);
+    else small_q.push_back(queries[i]);
+  }
+  int rc = GRUS_OK;
+  if (!small_q.empty()) {
+    rc = stage_tasks(b, small_q.data(), (int)small_q.size());
+    if (rc) return rc;
+  } else {
+    b->ntasks = b->nmembers = 0;
+  }
   const uint32_t nt = b->ntasks, nm = b->nmembers;
   const uint32_t *msrc = nm ? b->d_msrc : nullptr;
   const unsigned long long *moff = nm ? b->d_moff : nullptr;
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(b->ev0, s));
+  // queries on big graphs: whole-GPU launches queued first on the stream
+  uint32_t nerr = 0;
+  if (!big_q.empty()) {
+    if (b->err_cap < big_q.size()) {
+      if (b->h_errs) cudaFreeHost(b->h_errs);
+      b->h_errs = nullptr;
+      b->err_cap = 0;
+      GRUS_CUDA_TRY(cudaMallocHost(&b->h_errs, big_q.size() * 4));
+      b->err_cap = (uint32_t)big_q.size();
+    }
+    std::stable_sort(big_q.begin(), big_q.end(), [&](int x, int y) {
+      if (queries[x].graph != queries[y].graph) return queries[x].graph < queries[y].graph;
+      return queries[x].algo < queries[y].algo;
+    });
+    for (size_t i = 0; i < big_q.size();) {
+      const grus_query &q0 = queries[big_q[i]];
+      grus_graph *g = b->graphs[q0.graph];
+      size_t j = i + 1;
+      if (q0.algo == GRUS_ALGO_SSSP)
+        while (j < big_q.size() && j - i < 32 && queries[big_q[j]].graph == q0.graph &&
+               queries[big_q[j]].algo == GRUS_ALGO_SSSP)
+          ++j;
+      CtrlView cv;
+      if (j - i == 1) {
+        rc = q0.algo == GRUS_ALGO_SSSP ? grus_sssp(g, q0.src, out + q0.out_offset, nullptr, s)
+                                       : grus_bfs(g, q0.src, out + q0.out_offset, nullptr, s);
+        cv = q0.algo == GRUS_ALGO_SSSP ? sssp_ctrl(g) : bfs_ctrl(g);
+      } else {
+        uint32_t srcs[32];
+        uint32_t *outs[32];
+        for (size_t k = i; k < j; ++k) {
+          srcs[k - i] = queries[big_q[k]].src;
+          outs[k - i] = out + queries[big_q[k]].out_offset;
+        }
+        rc = msssp_run(g, srcs, (int)(j - i), outs, nullptr, s);
+        cv = msssp_ctrl(g);
+      }
+      if (rc) return rc;
+      if (cv.ctrl) {
+        GRUS_CUDA_TRY(cudaMemcpyAsync(b->h_errs + nerr, cv.ctrl + cv.err_off, 4,
+                                      cudaMemcpyDeviceToHost, s));
+        GRUS_CUDA_TRY(cudaMemsetAsync(cv.ctrl + cv.err_off, 0, 4, s));
+        ++nerr;
+      }
+      i = j;
+    }
+  }
+  if (nt == 0) {
+    // every query was on a big graph
+    if (stats) GRUS_CUDA_TRY(cudaEventRecord(b->ev1, s));
+    GRUS_CUDA_TRY(cudaEventRecord(b->done, s));
+    b->in_flight = true;
+    if (!stats) return GRUS_OK;
+    GRUS_CUDA_TRY(cudaStreamSynchronize(s));
+    uint32_t bits = 0;
+    for (uint32_t i = 0; i < nerr; ++i) bits |= b->h_errs[i];
+    if (bits) return status_from_device_error(bits);
+    std::memset(stats, 0, sizeof(*stats));
+    stats->kernel_launches = (uint32_t)big_q.size();
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    stats->device_ms = ms;
+    return GRUS_OK;
+  }
   if (use_graph) {
     // one captured graph per (task count, output buffer): H2D copy of the
     // staged tasks, counter reset, batch kernel
@@ -839,12 +928,13 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
   uint32_t err = 0;
   GRUS_CUDA_TRY(cudaMemcpyAsync(&err, b->state.err, 4, cudaMemcpyDeviceToHost, s));
   GRUS_CUDA_TRY(cudaStreamSynchronize(s));
+  for (uint32_t i = 0; i < nerr; ++i) err |= b->h_errs[i];
   if (err) {
     cudaMemset(b->state.err, 0, 4);
     return status_from_device_error(err);
   }
   std::memset(stats, 0, sizeof(*stats));
-  stats->kernel_launches = 1;
+  stats->kernel_launches = 1 + (uint32_t)big_q.size();
   float ms = 0.f;
   cudaEventElapsedTime(&ms, b->ev0, b->ev1);
   stats->device_ms = ms;
@@ -859,6 +949,7 @@ int grus_batch_get_info(const grus_batch *b, grus_batch_config *info) {
   info->huge_degree = b->huge;
   info->sssp_delta = b->delta;
   info->group_sources = b->group;
+  info->big_edges = b->big_edges >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)b->big_edges;
   return GRUS_OK;
 }
 
@@ -873,6 +964,7 @@ int grus_batch_free(grus_batch *b) {
   if (b->h_tasks) cudaFreeHost(b->h_tasks);
   cudaFree(b->d_msrc);
   cudaFree(b->d_moff);
+  if (b->h_errs) cudaFreeHost(b->h_errs);
   if (b->h_msrc) cudaFreeHost(b->h_msrc);
   if (b->h_moff) cudaFreeHost(b->h_moff);
   if (b->ev0) cudaEventDestroy(b->ev0);

@@ -69,7 +69,7 @@ struct grus_server {
   std::vector<uint8_t> big;  // per graph: served by the whole-GPU lane
   grus::GraphDesc *d_graphs = nullptr;
   uint64_t max_n = 0, max_m = 0;  // over the small graphs
-  uint64_t big_edges = 1ull << 24;
+  uint64_t big_edges = 1ull << 20;
   int cluster = 8;
   uint32_t huge = 1024, delta = 192;
   uint64_t reserve = 1ull << 30;

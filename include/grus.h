@@ -281,6 +281,11 @@ typedef struct grus_batch_config {
                             queries, so packing pays only when workers would
                             otherwise idle, e.g. many queries on few small
                             graphs) */
+  uint32_t big_edges;    /* queries on graphs with at least this many edges
+                            run as whole-GPU launches before the cluster
+                            workers start: SSSP packed 32 sources per
+                            launch, BFS one launch each (default 2^23;
+                            0xFFFFFFFF: never) */
 } grus_batch_config;
 
 typedef struct grus_batch grus_batch;
@@ -315,7 +320,7 @@ typedef struct grus_server_config {
   uint64_t hbm_reserve_bytes;/* free HBM kept back at admission (default 1 GiB) */
   uint32_t sssp_delta;
   uint32_t big_edges;        /* graphs with at least this many edges run on the
-                                whole-GPU lane (default 2^24; 0xFFFFFFFF: never) */
+                                whole-GPU lane (default 2^20; 0xFFFFFFFF: never) */
 } grus_server_config;
 
 typedef struct grus_completion {

@@ -138,3 +138,25 @@ def test_batch_sssp_groups(grus, graphs, group):
 def test_batch_rejects_bad_group_size(grus, graphs):
     with pytest.raises(grus.GrusError):
         grus.Batch(graphs, group_sources=33)
+
+
+@pytest.mark.parametrize("big_edges", [1 << 12, 1])
+def test_batch_big_graphs_run_whole_gpu(grus, graphs, big_edges):
+    """Queries on graphs at or above big_edges run as whole-GPU launches
+    before the cluster workers (all of them with big_edges=1); results equal
+    the single queries with plain launches and CUDA-graph replays."""
+    torch = pytest.importorskip("torch")
+    b = grus.Batch(graphs, big_edges=big_edges)
+    assert b.info()["big_edges"] == big_edges
+    queries = make_queries(grus, graphs, 80, 31 + big_edges)
+    queries += [(2, grus.ALGO_SSSP, s) for s in (0, 5, 77, 4000)]  # a pack on one graph
+    for use_graph in (False, True, True):
+        offs, total = b.layout(queries)
+        out = torch.full((total,), -5, dtype=torch.int32, device="cuda")
+        st = b.run(queries, out, offs, use_graph=use_graph, stats=True)
+        assert st["kernel_launches"] >= 1
+        res = out.cpu().numpy().view(np.uint32)
+        for q, o in zip(queries, offs):
+            ref = reference(grus, graphs, q)
+            assert np.array_equal(res[o:o + len(ref)], ref), (big_edges, use_graph, q)
+    b.free()
