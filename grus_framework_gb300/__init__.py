@@ -100,6 +100,15 @@ class ServerStats(C.Structure):
                 ("big_queries", C.c_uint64)]
 
 
+class Telemetry(C.Structure):
+    _fields_ = [("hbm_total_bytes", C.c_uint64), ("hbm_free_bytes", C.c_uint64),
+                ("link_tx_kbps", C.c_uint32), ("link_rx_kbps", C.c_uint32),
+                ("sm_clock_mhz", C.c_uint32), ("mem_clock_mhz", C.c_uint32),
+                ("power_mw", C.c_uint32), ("temperature_c", C.c_uint32),
+                ("valid", C.c_uint32), ("reserved", C.c_uint32),
+                ("driver_version", C.c_char * 32)]
+
+
 class Tuning(C.Structure):
     _fields_ = [
         ("alpha", C.c_float), ("beta", C.c_float), ("ctas_per_sm", C.c_uint32),
@@ -121,6 +130,9 @@ def _load():
         "grus_strerror": ([i32], C.c_char_p),
         "grus_last_error": ([], C.c_char_p),
         "grus_device_init": ([i32], i32),
+        "grus_convert_edgelist": ([C.c_char_p, C.c_char_p, C.c_uint32], i32),
+        "grus_save_result": ([C.c_char_p, vp, C.c_uint64, C.c_uint32], i32),
+        "grus_telemetry_sample": ([C.POINTER(Telemetry)], i32),
         "grus_check_wait_limit": ([C.c_uint32], i32),
         "grus_graph_from_csr": ([u64, u64, vp, vp, vp, u32, i32, u64, PG], i32),
         "grus_graph_load_gr": ([C.c_char_p, i32, i32, u64, PG], i32),
@@ -181,6 +193,52 @@ def _strerror(status):
 def _check(status, what):
     if status != 0:
         raise GrusError(status, what, lib.grus_last_error().decode())
+
+
+RESULT_U32, RESULT_F32 = 0, 1
+TEL_HBM, TEL_LINK, TEL_CLOCKS, TEL_POWER, TEL_TEMP, TEL_DRIVER = 1, 2, 4, 8, 16, 32
+RESULT_MAGIC = b"GRUSRES1"
+
+
+def convert_edgelist(in_path, out_path, symmetric=False, weighted=False) -> None:
+    """Edge list or Matrix Market coordinate file -> Galois .gr (include/grus.h
+    grus_convert_edgelist)."""
+    flags = (GEN_SYMMETRIC if symmetric else 0) | (GEN_WEIGHTED if weighted else 0)
+    _check(lib.grus_convert_edgelist(str(in_path).encode(), str(out_path).encode(), flags),
+           "grus_convert_edgelist")
+
+
+def save_result(path, values) -> None:
+    """Binary dump of a uint32/int32 or float32 result (numpy array or CUDA tensor)."""
+    dt = getattr(values, "dtype", None)
+    is_f32 = str(dt) in ("float32", "torch.float32")
+    n = values.numel() if hasattr(values, "numel") else int(values.size)
+    if not is_f32 and str(dt) not in ("uint32", "int32", "torch.int32"):
+        raise TypeError("results are 4-byte integers or float32")
+    if hasattr(values, "ctypes"):
+        values = np.ascontiguousarray(values)
+    _check(lib.grus_save_result(str(path).encode(), _ptr(values), n,
+                                RESULT_F32 if is_f32 else RESULT_U32), "grus_save_result")
+
+
+def load_result(path) -> np.ndarray:
+    """Reads a file written by save_result."""
+    raw = Path(path).read_bytes()
+    if raw[:8] != RESULT_MAGIC:
+        raise ValueError("not a result file")
+    typ, size = np.frombuffer(raw, np.uint32, 2, 8)
+    n = int(np.frombuffer(raw, np.uint64, 1, 16)[0])
+    return np.frombuffer(raw, np.float32 if typ == RESULT_F32 else np.uint32, n, 24).copy()
+
+
+def telemetry() -> dict:
+    """Device memory, host-link throughput, clocks, power and temperature of
+    the current device (fields present when the matching TEL_* bit is set)."""
+    t = Telemetry()
+    _check(lib.grus_telemetry_sample(C.byref(t)), "grus_telemetry_sample")
+    d = {k: getattr(t, k) for k, _ in t._fields_ if k != "reserved"}
+    d["driver_version"] = t.driver_version.decode(errors="replace")
+    return d
 
 
 def check_wait_limit(timeout_ms: int = 100) -> int:

@@ -40,6 +40,7 @@ SOURCES = [
     "batch.cu",
     "serve.cu",
     "tune.cu",
+    "tools.cu",
 ]
 
 
@@ -86,7 +87,7 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
                     print(" ".join(cmd), file=sys.stderr)
             list(ex.map(_run, jobs))
     if _stale(LIB, objs):
-        _run([cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-cudart", "static"])
+        _run([cc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-cudart", "static", "-ldl"])
     return LIB
 
 

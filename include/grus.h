@@ -300,6 +300,45 @@ GRUS_API int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, ui
 GRUS_API int grus_batch_get_info(const grus_batch *b, grus_batch_config *info);
 GRUS_API int grus_batch_free(grus_batch *b);
 
+/* ---- tooling ----------------------------------------------------------------- */
+/* Converts a text edge list ("u v [w]" per line, 0-based, '#' comments) or a
+ * Matrix Market coordinate file (1-based; "symmetric" in its header implies
+ * GRUS_GEN_SYMMETRIC, "pattern" drops weights) to the Galois v1 .gr layout.
+ * flags: GRUS_GEN_SYMMETRIC adds reverse edges and keeps one (u, v) per pair
+ * (the lightest); GRUS_GEN_WEIGHTED keeps the third column as uint32 weights
+ * (1 where absent).  The reference relies on Galois' graph-convert for this
+ * (README.md:14-27). */
+GRUS_API int grus_convert_edgelist(const char *in_path, const char *out_path, uint32_t flags);
+
+/* Binary dump of a result array (host or device): "GRUSRES1", uint32 type,
+ * uint32 element size (4), uint64 n, then the n values.  Beside the
+ * reference's text SaveResults (include/print.cuh:36-45). */
+#define GRUS_RESULT_U32 0u
+#define GRUS_RESULT_F32 1u
+GRUS_API int grus_save_result(const char *path, const void *values, uint64_t n, uint32_t type);
+
+/* Device telemetry of the current device, the quantities the reference's
+ * tools/pcie.py polls: device memory (CUDA), and through NVML, opened at run
+ * time, host-link throughput (NVML's PCIe counters, KB/s, sampled over about
+ * 20 ms), SM and memory clocks, power, temperature, driver version.  Only
+ * reads; `valid` tells which fields were available.  GRUS_ENODEV without a
+ * device. */
+#define GRUS_TEL_HBM 1u
+#define GRUS_TEL_LINK 2u
+#define GRUS_TEL_CLOCKS 4u
+#define GRUS_TEL_POWER 8u
+#define GRUS_TEL_TEMP 16u
+#define GRUS_TEL_DRIVER 32u
+typedef struct grus_telemetry {
+  uint64_t hbm_total_bytes, hbm_free_bytes;
+  uint32_t link_tx_kbps, link_rx_kbps;
+  uint32_t sm_clock_mhz, mem_clock_mhz;
+  uint32_t power_mw, temperature_c;
+  uint32_t valid, reserved;
+  char driver_version[32];
+} grus_telemetry;
+GRUS_API int grus_telemetry_sample(grus_telemetry *out);
+
 /* ---- serving --------------------------------------------------------------- */
 /* A query server over device-resident graphs.  Requests queue on the host
  * and are served by two lanes.  Small graphs (fewer than big_edges edges): a
