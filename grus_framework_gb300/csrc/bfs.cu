@@ -34,6 +34,12 @@
 //     m_f > m_u/alpha, pull->push when n_f < n/beta and the frontier shrinks;
 //     the first push level after a pull level turns the frontier bitmap into
 //     the queue with one atomic per CTA per 256 words.
+//   * narrow tail: a long traversal (64+ levels) whose push frontier and
+//     remaining edges have become small is handed to bfs_narrow, one CTA of
+//     1024 threads launched after the persistent kernel, which runs the last
+//     levels with block barriers, a shared-memory frontier and L1 prefetches
+//     of the next level's adjacency (about 3 µs per level against about 10 µs
+//     for a grid barrier level).
 // Depths are order-independent (every writer stores level+1), so results are
 // bit-exact against the serial oracle whatever the schedule.
 #include <algorithm>
@@ -51,6 +57,15 @@ constexpr uint32_t kDefHuge = 8192;   // chunking threshold
 constexpr uint32_t kDefBuScan = 8;    // pull: neighbours a lane checks alone
 constexpr uint32_t kDefBuWords = 4;   // pull: bitmap words per warp step
 constexpr float kDefAlpha = 15.f, kDefBeta = 18.f;
+// Narrow tail: a traversal still running after kNarrowAfter levels, with at
+// most kNarrowNf frontier vertices and at most kNarrowMu edges left whose
+// source is undiscovered, is finished by one 1024-thread CTA.  The edge bound
+// caps the work one SM may be left with (a few milliseconds at worst).
+constexpr uint32_t kNarrowAfter = 64;
+constexpr uint32_t kNarrowNf = 4096;
+constexpr uint64_t kNarrowMu = 1ull << 22;
+constexpr int kNarrowBlock = 1024;
+constexpr uint32_t kNarrowCap = 4096;   // shared-memory frontier entries per buffer
 
 struct LevelSlot {
   uint32_t qcount;         // queue entries of this level
@@ -64,6 +79,16 @@ struct LevelSlot {
 struct Summary {
   uint32_t levels, bu_levels, switches, pad;
   unsigned long long nr, mr;
+};
+
+// Hand-over from the persistent kernel to bfs_narrow (control block).
+struct Handover {
+  uint32_t flag;              // 1: bfs_narrow continues the traversal
+  uint32_t level;             // depth of the handed-over frontier
+  uint32_t nf;                // its queue entries (queue[qsel])
+  uint32_t qsel;
+  unsigned long long nr, mr;  // reach counts so far
+  uint32_t bu_levels, switches;
 };
 
 // Per-level record written by one thread after each level's barrier:
@@ -97,6 +122,8 @@ struct Args {
   LevelTrace *trace;      // optional (null: no trace)
   float alpha, beta;
   uint32_t huge, bu_scan;
+  uint32_t narrow_nf;     // hand over at most this many frontier vertices (0: never)
+  Handover *ho;
   uint64_t timeout_ns;
 };
 
@@ -118,7 +145,8 @@ struct Workspace {
 };
 
 constexpr size_t kOffSlots = 0, kOffBar = 256, kOffErr = 320, kOffSummary = 384,
-                 kCtrlBytes = 512;
+                 kOffHandover = 448, kCtrlBytes = 512;
+static_assert(kOffHandover + sizeof(Handover) <= kCtrlBytes, "hand-over overflows the control block");
 
 void ws_free(void *p) {
   Workspace *w = (Workspace *)p;
@@ -346,6 +374,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     const uint32_t words = (uint32_t)(a.front[2] - a.visited) + a.W;
     for (uint32_t i = gtid; i < words; i += nthreads) bm[i] = 0u;
     if (gtid < 4 * sizeof(LevelSlot) / 4) ((uint32_t *)a.slots)[gtid] = 0u;
+    if (gtid == 0 && a.ho) a.ho->flag = 0u;
   }
   if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
   const uint32_t sb = __ldg(a.offs + a.src), se = __ldg(a.offs + a.src + 1);
@@ -410,6 +439,34 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     } else {
       if ((double)NF * a.beta < (double)a.n && NF < prev_nf) nbu = false;
     }
+    if (a.narrow_nf && !bu && !nbu && L + 1 >= kNarrowAfter && NF <= a.narrow_nf &&
+        MF <= 16ull * a.narrow_nf && mu <= kNarrowMu && __ldcg(&nx->ccount) == 0) {
+      // A long traversal down to a small push frontier: every further level
+      // would be a grid barrier for a few thousand vertices.  Hand over to
+      // bfs_narrow (launched after this kernel).  Vertices unreached so far
+      // read INFINIT now; the narrow kernel writes the depth of each vertex it
+      // reaches later.
+      const uint32_t lane = lane_id();
+      const uint32_t gw = gtid >> 5, nw = nthreads >> 5;
+      for (uint32_t w = gw; w < a.W; w += nw) {
+        const uint32_t vis = __ldcg(a.visited + w);
+        const uint32_t v = w * 32 + lane;
+        if (!((vis >> lane) & 1u) && v < a.n) a.depth[v] = kInfinit;
+      }
+      if (gtid == 0) {
+        Handover *h = a.ho;
+        h->level = L + 1;
+        h->nf = min(__ldcg(&nx->qcount), a.queue_cap);
+        h->qsel = (L + 1) & 1u;
+        h->nr = nr;
+        h->mr = mr;
+        h->bu_levels = bu_levels;
+        h->switches = switches;
+        __threadfence();
+        h->flag = 1u;
+      }
+      return;
+    }
     from_pull = bu && !nbu;
     if (nbu != bu) ++switches;
     bu = nbu;
@@ -436,6 +493,219 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     a.summary->switches = switches;
     a.summary->nr = nr;
     a.summary->mr = mr;
+  }
+}
+
+// Starts filling this SM's L1 with the line holding p (no wait).
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+// Claims up to kNarrowBatch targets at once.  The chain per batch is short:
+// the column ids come from L1 (their lines were prefetched when their source
+// was discovered), the claiming atomicOr goes to L2 while the targets'
+// offsets are prefetched, and a new vertex's offsets then come from L1.  A
+// new vertex gets depth d and, if it has out-edges, a place in the next
+// frontier (shared memory first, then the global spill list as a vertex id)
+// and a prefetch of its first out-edges.
+constexpr int kNarrowBatch = 4;
+
+__device__ __forceinline__ void narrow_batch(const Args &a, const uint32_t (&xs)[kNarrowBatch],
+                                             int cnt, uint32_t d, uint2 *qn, uint32_t *cn,
+                                             uint32_t *spn, uint32_t *any, unsigned long long &nr,
+                                             unsigned long long &mr) {
+  uint32_t c[kNarrowBatch], old[kNarrowBatch];
+#pragma unroll
+  for (int r = 0; r < kNarrowBatch; ++r) c[r] = r < cnt ? __ldg(a.cols + xs[r]) : 0u;
+#pragma unroll
+  for (int r = 0; r < kNarrowBatch; ++r)
+    if (r < cnt) prefetch_l1(a.offs + c[r]);
+#pragma unroll
+  for (int r = 0; r < kNarrowBatch; ++r) {
+    const uint32_t bit = 1u << (c[r] & 31u);
+    old[r] = r < cnt ? atomicOr(a.visited + (c[r] >> 5), bit) : bit;
+  }
+#pragma unroll
+  for (int r = 0; r < kNarrowBatch; ++r) {
+    if (old[r] & (1u << (c[r] & 31u))) continue;
+    const uint32_t v = c[r];
+    a.depth[v] = d;
+    *any = 1u;
+    const uint32_t cb = __ldg(a.offs + v), ce = __ldg(a.offs + v + 1);
+    ++nr;
+    mr += ce - cb;
+    if (ce == cb) continue;
+    prefetch_l1(a.cols + cb);
+    prefetch_l1(a.cols + ce - 1);
+    const uint32_t pos = atomicAdd(cn, 1u);
+    if (pos < kNarrowCap) {
+      qn[pos] = make_uint2(cb, ce);
+    } else if (pos - kNarrowCap < a.queue_cap) {
+      spn[pos - kNarrowCap] = v;
+    } else {
+      atomicOr(a.err, kErrOverflow);
+    }
+  }
+}
+
+// The narrow tail of a long traversal: one CTA of 1024 threads takes the
+// small frontier the persistent kernel handed over and runs the remaining
+// levels with block barriers only.  A frontier entry is the (begin, end)
+// range of a vertex's out-edges, kept in shared memory (entries beyond
+// kNarrowCap spill to global memory as vertex ids).  Each level deals the
+// frontier's edges evenly to the threads (a block scan of the degrees and a
+// binary search for each thread's first entry), so a wide vertex is shared
+// by many threads, and each thread claims its edges in batches.  Returns at
+// once when the persistent kernel finished the traversal itself.
+__global__ void __launch_bounds__(kNarrowBlock) bfs_narrow(Args a) {
+  extern __shared__ uint2 s_q[];  // 2 * kNarrowCap entries
+  __shared__ uint32_t s_pref[kNarrowCap + 1];
+  __shared__ uint32_t s_cnt[2], s_any;
+  __shared__ unsigned long long s_red[kNarrowBlock / 32];
+  Handover *ho = a.ho;
+  if (__ldcg(&ho->flag) != 1u) return;
+  const uint32_t tid = threadIdx.x;
+  uint32_t d = __ldcg(&ho->level);  // depth of the current frontier
+  const uint32_t nf0 = __ldcg(&ho->nf);
+  const uint32_t *q0 = a.queue[__ldcg(&ho->qsel)];
+  uint32_t *spill[2] = {a.queue[0], a.queue[1]};
+  if (tid == 0) {
+    s_cnt[0] = 0;
+    s_cnt[1] = 0;
+    s_any = 0;
+  }
+  __syncthreads();
+  // the handed-over queue holds vertex ids: turn the ones with out-edges into
+  // ranges in buffer 0 (a copy, since queue[qsel] doubles as a spill list);
+  // every entry then has at least one edge, which the edge dealing relies on
+  for (uint32_t i = tid; i < nf0; i += kNarrowBlock) {
+    const uint32_t v = __ldcg(q0 + i);
+    const uint2 r = make_uint2(__ldg(a.offs + v), __ldg(a.offs + v + 1));
+    if (r.x == r.y) continue;
+    prefetch_l1(a.cols + r.x);
+    prefetch_l1(a.cols + r.y - 1);
+    const uint32_t pos = atomicAdd(&s_cnt[0], 1u);
+    if (pos < kNarrowCap) s_q[pos] = r;
+    else atomicOr(a.err, kErrOverflow);  // cannot happen: nf0 <= narrow_nf <= kNarrowCap
+  }
+  __syncthreads();
+  unsigned long long nr = 0, mr = 0;
+  uint32_t cur = 0, levels = 0;
+  constexpr uint32_t kPer = (kNarrowCap + kNarrowBlock - 1) / kNarrowBlock;
+  while (true) {
+    // the frontier at depth d is non-empty; `total` of its vertices have
+    // out-edges (clamped to what was stored: more already raised kErrOverflow)
+    const uint32_t total = min(s_cnt[cur], kNarrowCap + a.queue_cap);
+    if (total == 0) {
+      levels = d + 1;
+      break;
+    }
+    const uint32_t nxt = cur ^ 1u;
+    const uint32_t in_smem = min(total, kNarrowCap);
+    const uint2 *qc = s_q + cur * kNarrowCap;
+    uint2 *qn = s_q + nxt * kNarrowCap;
+    // exclusive prefix of the entries' degrees
+    const uint32_t e0 = tid * kPer;
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; ++k)
+      if (e0 + k < in_smem) sum += qc[e0 + k].y - qc[e0 + k].x;
+    uint32_t E = 0;
+    uint32_t run = block_exclusive_scan<kNarrowBlock>(sum, &E);
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; ++k)
+      if (e0 + k < in_smem) {
+        s_pref[e0 + k] = run;
+        run += qc[e0 + k].y - qc[e0 + k].x;
+      }
+    if (tid == 0) s_pref[in_smem] = E;
+    __syncthreads();
+    // this thread's edges [lo, hi) of the E in shared-memory entries
+    const uint32_t lo = (uint32_t)((unsigned long long)tid * E / kNarrowBlock);
+    const uint32_t hi = (uint32_t)((unsigned long long)(tid + 1) * E / kNarrowBlock);
+    if (lo < hi) {
+      uint32_t j = 0, span = in_smem;  // largest j with s_pref[j] <= lo
+      while (span > 1) {
+        const uint32_t half = span / 2;
+        if (s_pref[j + half] <= lo) j += half;
+        span -= half;
+      }
+      uint32_t x = qc[j].x + (lo - s_pref[j]);
+      uint32_t xe = qc[j].y;
+      for (uint32_t k = lo; k < hi; k += kNarrowBatch) {
+        const int cnt = (int)min(hi - k, (uint32_t)kNarrowBatch);
+        uint32_t xs[kNarrowBatch];
+#pragma unroll
+        for (int r = 0; r < kNarrowBatch; ++r) {
+          xs[r] = x;
+          if (r < cnt && ++x == xe && k + r + 1 < hi) {
+            ++j;
+            x = qc[j].x;
+            xe = qc[j].y;
+          }
+        }
+        narrow_batch(a, xs, cnt, d + 1, qn, &s_cnt[nxt], spill[nxt], &s_any, nr, mr);
+      }
+    }
+    // spilled entries (rare: a frontier beyond kNarrowCap), one vertex per thread
+    for (uint32_t i = in_smem + tid; i < total; i += kNarrowBlock) {
+      const uint32_t v = __ldcg(spill[cur] + (i - in_smem));
+      const uint32_t b = __ldg(a.offs + v), e = __ldg(a.offs + v + 1);
+      for (uint32_t x = b; x < e; x += kNarrowBatch) {
+        const int cnt = (int)min(e - x, (uint32_t)kNarrowBatch);
+        uint32_t xs[kNarrowBatch];
+#pragma unroll
+        for (int r = 0; r < kNarrowBatch; ++r) xs[r] = x + r;
+        narrow_batch(a, xs, cnt, d + 1, qn, &s_cnt[nxt], spill[nxt], &s_any, nr, mr);
+      }
+    }
+    __syncthreads();
+    const bool found = s_any != 0;
+    if (tid == 0 && a.trace && d + 1 < (uint32_t)kMaxTrace)
+      a.trace[d + 1] = LevelTrace{global_timer_ns(), (unsigned long long)E,
+                                  min(s_cnt[nxt], a.n), 0u};
+    __syncthreads();  // every thread has read s_any and the counts
+    if (!found) {
+      levels = d + 1;  // nothing at depth d + 1
+      break;
+    }
+    if (tid == 0) {
+      s_cnt[cur] = 0;
+      s_any = 0;
+    }
+    ++d;
+    cur = nxt;
+    if (d > a.n + 1) {
+      if (tid == 0) atomicOr(a.err, kErrLevels);
+      levels = d;
+      break;
+    }
+    __syncthreads();
+  }
+// reach counts: this kernel's share plus the persistent kernel's
+  for (int o = 16; o > 0; o >>= 1) {
+    nr += __shfl_down_sync(0xffffffffu, nr, o);
+    mr += __shfl_down_sync(0xffffffffu, mr, o);
+  }
+  if ((tid & 31u) == 0) s_red[tid >> 5] = nr;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long t = 0;
+    for (int i = 0; i < kNarrowBlock / 32; ++i) t += s_red[i];
+    a.summary->nr = __ldcg(&ho->nr) + t;
+  }
+  __syncthreads();
+  if ((tid & 31u) == 0) s_red[tid >> 5] = mr;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long t = 0;
+    for (int i = 0; i < kNarrowBlock / 32; ++i) t += s_red[i];
+    a.summary->mr = __ldcg(&ho->mr) + t;
+    a.summary->levels = levels;
+    a.summary->bu_levels = __ldcg(&ho->bu_levels);
+    a.summary->switches = __ldcg(&ho->switches);
+    a.summary->pad = __ldcg(&ho->level);  // level of the hand-over
+    ho->flag = 0u;
   }
 }
 
@@ -513,7 +783,15 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   a.beta = tune_or(g->tuning.beta, kDefBeta);
   a.huge = tune_or(g->tuning.huge_degree, kDefHuge);
   a.bu_scan = tune_or(g->tuning.bu_scan, kDefBuScan);
+  a.narrow_nf = kNarrowNf;
+  a.ho = (Handover *)(w->ctrl + kOffHandover);
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
+  static int narrow_ready = 0;
+  if (!narrow_ready) {
+    GRUS_CUDA_TRY(cudaFuncSetAttribute(bfs_narrow, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(2 * kNarrowCap * sizeof(uint2))));
+    narrow_ready = 1;
+  }
 
   cudaLaunchAttribute attrs[2];
   int nattr = 0;
@@ -542,6 +820,10 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   const bool sync = stats != nullptr || !dev_out;
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
   GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a));
+  // continues a long traversal the persistent kernel handed over; returns at
+  // once otherwise
+  bfs_narrow<<<1, kNarrowBlock, 2 * kNarrowCap * sizeof(uint2), s>>>(a);
+  GRUS_CUDA_TRY(cudaGetLastError());
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev1, s));
   if (!dev_out) GRUS_CUDA_TRY(cudaMemcpyAsync(depth, w->depth, g->n * 4, cudaMemcpyDeviceToHost, s));
   if (!sync) return GRUS_OK;
@@ -563,7 +845,7 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
     stats->levels = sm->levels;
     stats->bottom_up_levels = sm->bu_levels;
     stats->direction_switches = sm->switches;
-    stats->kernel_launches = 1;
+    stats->kernel_launches = 2;
     stats->vertices_reached = sm->nr;
     stats->edges_reached = sm->mr;
     float ms = 0.f;

@@ -133,3 +133,50 @@ def test_bfs_errors(grus):
 def test_bfs_rmat22_full_size(grus, oracle_mod):
     g = grus.Graph.rmat(22, 16, 2, symmetric=True)
     _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex])
+
+
+def _broom(path_len, leaves):
+    """A path 0..path_len-1, a star of `leaves` leaves on its last vertex,
+    and one further vertex behind every leaf (symmetric CSR)."""
+    edges = [(i, i + 1) for i in range(path_len - 1)]
+    hub = path_len - 1
+    for k in range(leaves):
+        leaf = path_len + k
+        edges.append((hub, leaf))
+        edges.append((leaf, path_len + leaves + k))
+    n = path_len + 2 * leaves
+    both = edges + [(v, u) for u, v in edges]
+    both.sort()
+    offs = np.zeros(n + 1, np.uint32)
+    for u, _ in both:
+        offs[u + 1] += 1
+    offs = np.cumsum(offs).astype(np.uint32)
+    cols = np.array([v for _, v in both], np.uint32)
+    return offs, cols
+
+
+def test_bfs_long_tail_wide_vertex_and_spill(grus, oracle_mod):
+    """A traversal past the hand-over level with a small frontier finishes in
+    the single-CTA tail; there the edges of a vertex of degree 10,000 are
+    dealt to all of the CTA's threads and its 10,000 neighbours overflow the
+    shared-memory frontier into the spill list.  Depths and counts equal the
+    oracle's."""
+    offs, cols = _broom(200, 10000)
+    g = grus.Graph.from_csr(offs, cols, symmetric=True)
+    _check_bfs(grus, oracle_mod, g, [0, 150, 199, 200 + 10000 + 5])
+
+
+def test_bfs_long_tail_with_sinks(grus, oracle_mod):
+    """A directed comb: a 300-vertex path whose every vertex also points at a
+    sink of out-degree 0, so the frontiers the single-CTA tail takes over and
+    builds hold vertices without out-edges."""
+    path = 300
+    offs = np.zeros(2 * path + 1, np.uint32)
+    cols = []
+    for i in range(path):
+        nb = [path + i] + ([i + 1] if i + 1 < path else [])
+        cols.extend(nb)
+        offs[i + 1] = offs[i] + len(nb)
+    offs[path + 1:] = offs[path]
+    g = grus.Graph.from_csr(offs, np.array(cols, np.uint32))
+    _check_bfs(grus, oracle_mod, g, [0, 7, path - 1, path + 3])
