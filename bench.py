@@ -65,7 +65,8 @@ WORKLOADS = {
     "pagerank-rmat24": dict(algo="pagerank", graph="rmat", scale=24, edge_factor=16, seed=3,
                             symmetric=False, weighted=False, kernel="pr_persistent", iters=20,
                             metric="GTEPS (pull PageRank, 20 iterations, RMAT-24 directed)"),
-    "bfs-grid4096": dict(algo="bfs", graph="grid", scale=12, seed=0, kernel="bfs_persistent",
+    "bfs-grid4096": dict(algo="bfs", graph="grid", scale=12, seed=0,
+                         kernel="bfs_persistent+bfs_narrow",
                          metric="GTEPS (single-query BFS, 4096x4096 grid, source 4097)"),
     "msbfs-rmat23": dict(algo="msbfs", graph="rmat", scale=23, edge_factor=16, seed=4,
                          symmetric=True, weighted=False, kernel="msbfs_persistent", sources=64,

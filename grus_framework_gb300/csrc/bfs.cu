@@ -35,11 +35,12 @@
 //     the first push level after a pull level turns the frontier bitmap into
 //     the queue with one atomic per CTA per 256 words.
 //   * narrow tail: a long traversal (64+ levels) whose push frontier and
-//     remaining edges have become small is handed to bfs_narrow, one CTA of
-//     1024 threads launched after the persistent kernel, which runs the last
-//     levels with block barriers, a shared-memory frontier and L1 prefetches
-//     of the next level's adjacency (about 3 µs per level against about 10 µs
-//     for a grid barrier level).
+//     remaining edges have become small is handed to bfs_narrow, a cluster of
+//     up to 16 CTAs of 1024 threads launched after the persistent kernel,
+//     which runs the remaining levels with one hardware cluster barrier each,
+//     frontiers in distributed shared memory and prefetches of the next
+//     level's adjacency (about 3.3 µs per level against 9-10 µs for a grid
+//     barrier level).
 // Depths are order-independent (every writer stores level+1), so results are
 // bit-exact against the serial oracle whatever the schedule.
 #include <algorithm>
@@ -51,21 +52,25 @@
 namespace grus {
 namespace {
 
+namespace cg = cooperative_groups;
+
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 constexpr uint32_t kDefHuge = 8192;   // chunking threshold
 constexpr uint32_t kDefBuScan = 8;    // pull: neighbours a lane checks alone
 constexpr uint32_t kDefBuWords = 4;   // pull: bitmap words per warp step
 constexpr float kDefAlpha = 15.f, kDefBeta = 18.f;
-// Narrow tail: a traversal still running after kNarrowAfter levels, with at
-// most kNarrowNf frontier vertices and at most kNarrowMu edges left whose
-// source is undiscovered, is finished by one 1024-thread CTA.  The edge bound
-// caps the work one SM may be left with (a few milliseconds at worst).
+// Narrow tail: a traversal still running after kNarrowAfter levels, with a
+// push frontier of at most kNarrowNf vertices per tail CTA and at most
+// kNarrowMu edges left whose source is undiscovered, is finished by one
+// thread-block cluster of up to 16 CTAs of 1024 threads.  The edge bound caps
+// the work the cluster may be left with.
 constexpr uint32_t kNarrowAfter = 64;
 constexpr uint32_t kNarrowNf = 4096;
-constexpr uint64_t kNarrowMu = 1ull << 22;
+constexpr uint64_t kNarrowMu = 1ull << 26;
 constexpr int kNarrowBlock = 1024;
-constexpr uint32_t kNarrowCap = 4096;   // shared-memory frontier entries per buffer
+constexpr int kNarrowMaxCluster = 16;
+constexpr uint32_t kNarrowCap = 4096;   // shared-memory frontier entries per buffer per CTA
 
 struct LevelSlot {
   uint32_t qcount;         // queue entries of this level
@@ -89,6 +94,7 @@ struct Handover {
   uint32_t qsel;
   unsigned long long nr, mr;  // reach counts so far
   uint32_t bu_levels, switches;
+  uint32_t spill[3];          // spilled frontier entries, by depth mod 3
 };
 
 // Per-level record written by one thread after each level's barrier:
@@ -496,23 +502,41 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
   }
 }
 
-// Starts filling this SM's L1 with the line holding p (no wait).
+// Starts filling this SM's L1 (or only L2) with the line holding p (no wait).
 __device__ __forceinline__ void prefetch_l1(const void *p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// Per-level state of the tail cluster.  Every frontier vertex has an owner
+// CTA (a hash of its id); the owner keeps it as the (begin, end) range of its
+// out-edges in shared memory, or -- beyond kNarrowCap entries -- the vertex id
+// goes to a global spill list shared by the cluster.
+struct Tail {
+  cg::cluster_group cl;
+  uint32_t rank, C;
+  uint2 *q;            // this CTA's 2 * kNarrowCap entries
+  uint32_t *cnt;       // this CTA's 2 entry counters
+  uint32_t *found;     // this CTA's flag: it found a vertex at this level
+};
+
+__device__ __forceinline__ uint32_t tail_owner(uint32_t v, uint32_t C) {
+  return __umulhi(v * 2654435761u, C);
+}
 
 // Claims up to kNarrowBatch targets at once.  The chain per batch is short:
-// the column ids come from L1 (their lines were prefetched when their source
-// was discovered), the claiming atomicOr goes to L2 while the targets'
-// offsets are prefetched, and a new vertex's offsets then come from L1.  A
-// new vertex gets depth d and, if it has out-edges, a place in the next
-// frontier (shared memory first, then the global spill list as a vertex id)
-// and a prefetch of its first out-edges.
+// the column ids come from L1 (their lines were prefetched), the claiming
+// atomicOr goes to L2 while the targets' offsets are prefetched, and a new
+// vertex's offsets then come from L1.  A new vertex gets depth d and, if it
+// has out-edges, a place in its owner's next frontier and a prefetch of its
+// first out-edges.
 constexpr int kNarrowBatch = 4;
 
-__device__ __forceinline__ void narrow_batch(const Args &a, const uint32_t (&xs)[kNarrowBatch],
-                                             int cnt, uint32_t d, uint2 *qn, uint32_t *cn,
-                                             uint32_t *spn, uint32_t *any, unsigned long long &nr,
+__device__ __forceinline__ void narrow_batch(const Args &a, Tail &t,
+                                             const uint32_t (&xs)[kNarrowBatch], int cnt,
+                                             uint32_t d, uint32_t nxt, unsigned long long &nr,
                                              unsigned long long &mr) {
   uint32_t c[kNarrowBatch], old[kNarrowBatch];
 #pragma unroll
@@ -530,86 +554,107 @@ __device__ __forceinline__ void narrow_batch(const Args &a, const uint32_t (&xs)
     if (old[r] & (1u << (c[r] & 31u))) continue;
     const uint32_t v = c[r];
     a.depth[v] = d;
-    *any = 1u;
     const uint32_t cb = __ldg(a.offs + v), ce = __ldg(a.offs + v + 1);
     ++nr;
     mr += ce - cb;
+    *t.found = 1u;
     if (ce == cb) continue;
-    prefetch_l1(a.cols + cb);
-    prefetch_l1(a.cols + ce - 1);
-    const uint32_t pos = atomicAdd(cn, 1u);
-    if (pos < kNarrowCap) {
-      qn[pos] = make_uint2(cb, ce);
-    } else if (pos - kNarrowCap < a.queue_cap) {
-      spn[pos - kNarrowCap] = v;
+    const uint32_t o = tail_owner(v, t.C);
+    if (o == t.rank) {
+      prefetch_l1(a.cols + cb);
+      prefetch_l1(a.cols + ce - 1);
     } else {
-      atomicOr(a.err, kErrOverflow);
+      prefetch_l2(a.cols + cb);
+      prefetch_l2(a.cols + ce - 1);
+    }
+    // one reservation per owner among the lanes pushing together
+    cg::coalesced_group pg = cg::coalesced_threads();
+    cg::coalesced_group peers = cg::labeled_partition(pg, o);
+    uint32_t base = 0;
+    if (peers.thread_rank() == 0) base = atomicAdd(t.cl.map_shared_rank(t.cnt + nxt, o), peers.size());
+    const uint32_t pos = peers.shfl(base, 0) + peers.thread_rank();
+    if (pos < kNarrowCap) {
+      t.cl.map_shared_rank(t.q, o)[nxt * kNarrowCap + pos] = make_uint2(cb, ce);
+    } else {
+      const uint32_t g = atomicAdd(&a.ho->spill[d % 3], 1u);
+      if (g < a.queue_cap) a.queue[d & 1u][g] = v;
+      else atomicOr(a.err, kErrOverflow);  // cannot happen: spilled vertices are distinct
     }
   }
 }
 
-// The narrow tail of a long traversal: one CTA of 1024 threads takes the
-// small frontier the persistent kernel handed over and runs the remaining
-// levels with block barriers only.  A frontier entry is the (begin, end)
-// range of a vertex's out-edges, kept in shared memory (entries beyond
-// kNarrowCap spill to global memory as vertex ids).  Each level deals the
-// frontier's edges evenly to the threads (a block scan of the degrees and a
-// binary search for each thread's first entry), so a wide vertex is shared
-// by many threads, and each thread claims its edges in batches.  Returns at
-// once when the persistent kernel finished the traversal itself.
+// The narrow tail of a long traversal: one cluster of C CTAs (1 <= C <= 16)
+// of 1024 threads takes the small frontier the persistent kernel handed over
+// and runs the remaining levels with one hardware cluster barrier per level.
+// Each CTA deals the edges of the frontier vertices it owns evenly to its
+// threads (a block scan of the degrees and a binary search for each thread's
+// first entry), so a wide vertex is shared by many threads, and each thread
+// claims its edges in batches; spilled entries are dealt over the whole
+// cluster one vertex per thread.  A CTA that found a vertex writes the new
+// depth into every CTA's stamp before the level's barrier, so after it each
+// CTA reads its own stamp; stamps only grow, so no CTA has to clear them.
+// Returns at once when the persistent kernel finished the traversal itself.
 __global__ void __launch_bounds__(kNarrowBlock) bfs_narrow(Args a) {
   extern __shared__ uint2 s_q[];  // 2 * kNarrowCap entries
   __shared__ uint32_t s_pref[kNarrowCap + 1];
-  __shared__ uint32_t s_cnt[2], s_any;
+  __shared__ uint32_t s_cnt[2], s_found, s_stamp;
   __shared__ unsigned long long s_red[kNarrowBlock / 32];
   Handover *ho = a.ho;
-  if (__ldcg(&ho->flag) != 1u) return;
+  if (__ldcg(&ho->flag) != 1u) return;  // the same answer in every CTA
+  Tail t{cg::this_cluster(), 0, 1, s_q, s_cnt, &s_found};
+  t.rank = t.cl.block_rank();
+  t.C = t.cl.num_blocks();
   const uint32_t tid = threadIdx.x;
   uint32_t d = __ldcg(&ho->level);  // depth of the current frontier
+  const uint32_t d0 = d;
   const uint32_t nf0 = __ldcg(&ho->nf);
   const uint32_t *q0 = a.queue[__ldcg(&ho->qsel)];
-  uint32_t *spill[2] = {a.queue[0], a.queue[1]};
   if (tid == 0) {
     s_cnt[0] = 0;
     s_cnt[1] = 0;
-    s_any = 0;
+    s_found = 0;
+    s_stamp = d;
+    if (t.rank == 0) {
+      ho->spill[d % 3] = 0u;  // the counters of depths d0 and d0 + 1
+      ho->spill[(d + 1) % 3] = 0u;
+      a.summary->nr = __ldcg(&ho->nr);
+      a.summary->mr = __ldcg(&ho->mr);
+      if (a.trace && d + 1 < (uint32_t)kMaxTrace) a.trace[d + 1] = LevelTrace{0ull, 0ull, 0u, 0u};
+    }
   }
   __syncthreads();
-  // the handed-over queue holds vertex ids: turn the ones with out-edges into
-  // ranges in buffer 0 (a copy, since queue[qsel] doubles as a spill list);
-  // every entry then has at least one edge, which the edge dealing relies on
-  for (uint32_t i = tid; i < nf0; i += kNarrowBlock) {
+  // this CTA's share of the handed-over queue (vertex ids) becomes ranges in
+  // buffer 0; vertices without out-edges are left out, so every entry has at
+  // least one edge, which the edge dealing relies on
+  for (uint32_t i = t.rank + t.C * tid; i < nf0; i += t.C * kNarrowBlock) {
     const uint32_t v = __ldcg(q0 + i);
     const uint2 r = make_uint2(__ldg(a.offs + v), __ldg(a.offs + v + 1));
     if (r.x == r.y) continue;
-    prefetch_l1(a.cols + r.x);
-    prefetch_l1(a.cols + r.y - 1);
     const uint32_t pos = atomicAdd(&s_cnt[0], 1u);
     if (pos < kNarrowCap) s_q[pos] = r;
-    else atomicOr(a.err, kErrOverflow);  // cannot happen: nf0 <= narrow_nf <= kNarrowCap
+    else atomicOr(a.err, kErrOverflow);  // cannot happen: nf0 <= C * kNarrowCap
   }
-  __syncthreads();
+  t.cl.sync();  // every CTA's counters are set before any remote push
   unsigned long long nr = 0, mr = 0;
   uint32_t cur = 0, levels = 0;
   constexpr uint32_t kPer = (kNarrowCap + kNarrowBlock - 1) / kNarrowBlock;
   while (true) {
-    // the frontier at depth d is non-empty; `total` of its vertices have
-    // out-edges (clamped to what was stored: more already raised kErrOverflow)
-    const uint32_t total = min(s_cnt[cur], kNarrowCap + a.queue_cap);
-    if (total == 0) {
-      levels = d + 1;
-      break;
-    }
     const uint32_t nxt = cur ^ 1u;
-    const uint32_t in_smem = min(total, kNarrowCap);
+    const uint32_t in_smem = min(s_cnt[cur], kNarrowCap);
+    // entries spilled into the frontier at depth d
+    const uint32_t spilled = min(__ldcg(&ho->spill[d % 3]), a.queue_cap);
     const uint2 *qc = s_q + cur * kNarrowCap;
-    uint2 *qn = s_q + nxt * kNarrowCap;
-    // exclusive prefix of the entries' degrees
+    // exclusive prefix of the entries' degrees; the first line of each
+    // entry's adjacency is pulled into L1 meanwhile
     const uint32_t e0 = tid * kPer;
     uint32_t sum = 0;
 #pragma unroll
     for (uint32_t k = 0; k < kPer; ++k)
-      if (e0 + k < in_smem) sum += qc[e0 + k].y - qc[e0 + k].x;
+      if (e0 + k < in_smem) {
+        const uint2 r = qc[e0 + k];
+        prefetch_l1(a.cols + r.x);
+        sum += r.y - r.x;
+      }
     uint32_t E = 0;
     uint32_t run = block_exclusive_scan<kNarrowBlock>(sum, &E);
 #pragma unroll
@@ -618,8 +663,21 @@ __global__ void __launch_bounds__(kNarrowBlock) bfs_narrow(Args a) {
         s_pref[e0 + k] = run;
         run += qc[e0 + k].y - qc[e0 + k].x;
       }
-    if (tid == 0) s_pref[in_smem] = E;
+    if (tid == 0) {
+      s_pref[in_smem] = E;
+      // the spill counter for depth d + 2 is reused: its last readers
+      // finished before the previous cluster barrier
+      if (t.rank == 0) {
+        ho->spill[(d + 2) % 3] = 0u;
+        if (a.trace && d + 2 < (uint32_t)kMaxTrace) a.trace[d + 2] = LevelTrace{0ull, 0ull, 0u, 0u};
+      }
+      if (a.trace && d + 1 < (uint32_t)kMaxTrace) {
+        atomicAdd(&a.trace[d + 1].mf, (unsigned long long)E);
+        atomicAdd(&a.trace[d + 1].nf, in_smem);
+      }
+    }
     __syncthreads();
+    if (tid == 0) s_cnt[cur] = 0;  // read by every thread above; refilled next level
     // this thread's edges [lo, hi) of the E in shared-memory entries
     const uint32_t lo = (uint32_t)((unsigned long long)tid * E / kNarrowBlock);
     const uint32_t hi = (uint32_t)((unsigned long long)(tid + 1) * E / kNarrowBlock);
@@ -644,45 +702,46 @@ __global__ void __launch_bounds__(kNarrowBlock) bfs_narrow(Args a) {
             xe = qc[j].y;
           }
         }
-        narrow_batch(a, xs, cnt, d + 1, qn, &s_cnt[nxt], spill[nxt], &s_any, nr, mr);
+        narrow_batch(a, t, xs, cnt, d + 1, nxt, nr, mr);
       }
     }
-    // spilled entries (rare: a frontier beyond kNarrowCap), one vertex per thread
-    for (uint32_t i = in_smem + tid; i < total; i += kNarrowBlock) {
-      const uint32_t v = __ldcg(spill[cur] + (i - in_smem));
-      const uint32_t b = __ldg(a.offs + v), e = __ldg(a.offs + v + 1);
-      for (uint32_t x = b; x < e; x += kNarrowBatch) {
-        const int cnt = (int)min(e - x, (uint32_t)kNarrowBatch);
-        uint32_t xs[kNarrowBatch];
+    // spilled entries (rare: a frontier beyond C * kNarrowCap), one vertex
+    // per thread over the whole cluster
+    if (spilled) {
+      const uint32_t *sp = a.queue[d & 1u];
+      for (uint32_t i = t.rank * kNarrowBlock + tid; i < spilled; i += t.C * kNarrowBlock) {
+        const uint32_t v = __ldcg(sp + i);
+        const uint32_t b = __ldg(a.offs + v), e = __ldg(a.offs + v + 1);
+        for (uint32_t x = b; x < e; x += kNarrowBatch) {
+          const int cnt = (int)min(e - x, (uint32_t)kNarrowBatch);
+          uint32_t xs[kNarrowBatch];
 #pragma unroll
-        for (int r = 0; r < kNarrowBatch; ++r) xs[r] = x + r;
-        narrow_batch(a, xs, cnt, d + 1, qn, &s_cnt[nxt], spill[nxt], &s_any, nr, mr);
+          for (int r = 0; r < kNarrowBatch; ++r) xs[r] = x + r;
+          narrow_batch(a, t, xs, cnt, d + 1, nxt, nr, mr);
+        }
       }
     }
     __syncthreads();
-    const bool found = s_any != 0;
-    if (tid == 0 && a.trace && d + 1 < (uint32_t)kMaxTrace)
-      a.trace[d + 1] = LevelTrace{global_timer_ns(), (unsigned long long)E,
-                                  min(s_cnt[nxt], a.n), 0u};
-    __syncthreads();  // every thread has read s_any and the counts
+    if (tid < t.C && s_found) *t.cl.map_shared_rank(&s_stamp, tid) = d + 1;
+    // every push and stamp of this level is visible after the barrier
+    t.cl.sync();
+    if (tid == 0) s_found = 0;  // set again at the next level, after its scan barriers
+    const bool found = s_stamp > d;  // stamps only grow: a faster CTA may already write d + 2
+    if (t.rank == 0 && tid == 0 && a.trace && d + 1 < (uint32_t)kMaxTrace)
+      a.trace[d + 1].t_ns = global_timer_ns();
     if (!found) {
       levels = d + 1;  // nothing at depth d + 1
       break;
     }
-    if (tid == 0) {
-      s_cnt[cur] = 0;
-      s_any = 0;
-    }
     ++d;
     cur = nxt;
     if (d > a.n + 1) {
-      if (tid == 0) atomicOr(a.err, kErrLevels);
+      if (t.rank == 0 && tid == 0) atomicOr(a.err, kErrLevels);
       levels = d;
       break;
     }
-    __syncthreads();
   }
-// reach counts: this kernel's share plus the persistent kernel's
+  // reach counts: the persistent kernel's share (set above) plus each CTA's
   for (int o = 16; o > 0; o >>= 1) {
     nr += __shfl_down_sync(0xffffffffu, nr, o);
     mr += __shfl_down_sync(0xffffffffu, mr, o);
@@ -690,23 +749,57 @@ __global__ void __launch_bounds__(kNarrowBlock) bfs_narrow(Args a) {
   if ((tid & 31u) == 0) s_red[tid >> 5] = nr;
   __syncthreads();
   if (tid == 0) {
-    unsigned long long t = 0;
-    for (int i = 0; i < kNarrowBlock / 32; ++i) t += s_red[i];
-    a.summary->nr = __ldcg(&ho->nr) + t;
+    unsigned long long v = 0;
+    for (int i = 0; i < kNarrowBlock / 32; ++i) v += s_red[i];
+    atomicAdd(&a.summary->nr, v);
   }
   __syncthreads();
   if ((tid & 31u) == 0) s_red[tid >> 5] = mr;
   __syncthreads();
   if (tid == 0) {
-    unsigned long long t = 0;
-    for (int i = 0; i < kNarrowBlock / 32; ++i) t += s_red[i];
-    a.summary->mr = __ldcg(&ho->mr) + t;
-    a.summary->levels = levels;
-    a.summary->bu_levels = __ldcg(&ho->bu_levels);
-    a.summary->switches = __ldcg(&ho->switches);
-    a.summary->pad = __ldcg(&ho->level);  // level of the hand-over
-    ho->flag = 0u;
+    unsigned long long v = 0;
+    for (int i = 0; i < kNarrowBlock / 32; ++i) v += s_red[i];
+    atomicAdd(&a.summary->mr, v);
+    if (t.rank == 0) {
+      a.summary->levels = levels;
+      a.summary->bu_levels = __ldcg(&ho->bu_levels);
+      a.summary->switches = __ldcg(&ho->switches);
+      a.summary->pad = d0;  // level of the hand-over
+    }
   }
+  // no CTA leaves while another may still write its shared memory
+  t.cl.sync();
+  if (t.rank == 0 && tid == 0) ho->flag = 0u;
+}
+
+constexpr size_t kNarrowSmem = 2 * kNarrowCap * sizeof(uint2);
+
+// The largest cluster of bfs_narrow CTAs (16, 8, 4, 2 or 1) the device can
+// co-schedule, decided once per process; 1 needs no cluster launch.
+int narrow_cluster() {
+  static const int c = [] {
+    cudaFuncSetAttribute(bfs_narrow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNarrowSmem);
+    cudaFuncSetAttribute(bfs_narrow, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (int k = kNarrowMaxCluster; k > 1; k /= 2) {
+      cudaLaunchAttribute attr;
+      attr.id = cudaLaunchAttributeClusterDimension;
+      attr.val.clusterDim.x = (unsigned)k;
+      attr.val.clusterDim.y = 1;
+      attr.val.clusterDim.z = 1;
+      cudaLaunchConfig_t cfg;
+      std::memset(&cfg, 0, sizeof(cfg));
+      cfg.gridDim = dim3((unsigned)k);
+      cfg.blockDim = dim3(kNarrowBlock);
+      cfg.dynamicSmemBytes = kNarrowSmem;
+      cfg.attrs = &attr;
+      cfg.numAttrs = 1;
+      int nc = 0;
+      if (cudaOccupancyMaxActiveClusters(&nc, bfs_narrow, &cfg) == cudaSuccess && nc >= 1) return k;
+      cudaGetLastError();
+    }
+    return 1;
+  }();
+  return c;
 }
 
 }  // namespace
@@ -783,15 +876,10 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   a.beta = tune_or(g->tuning.beta, kDefBeta);
   a.huge = tune_or(g->tuning.huge_degree, kDefHuge);
   a.bu_scan = tune_or(g->tuning.bu_scan, kDefBuScan);
-  a.narrow_nf = kNarrowNf;
+  const int ncl = narrow_cluster();
+  a.narrow_nf = kNarrowNf * (uint32_t)ncl;
   a.ho = (Handover *)(w->ctrl + kOffHandover);
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
-  static int narrow_ready = 0;
-  if (!narrow_ready) {
-    GRUS_CUDA_TRY(cudaFuncSetAttribute(bfs_narrow, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(2 * kNarrowCap * sizeof(uint2))));
-    narrow_ready = 1;
-  }
 
   cudaLaunchAttribute attrs[2];
   int nattr = 0;
@@ -822,8 +910,22 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a));
   // continues a long traversal the persistent kernel handed over; returns at
   // once otherwise
-  bfs_narrow<<<1, kNarrowBlock, 2 * kNarrowCap * sizeof(uint2), s>>>(a);
-  GRUS_CUDA_TRY(cudaGetLastError());
+  {
+    cudaLaunchAttribute cattr;
+    cattr.id = cudaLaunchAttributeClusterDimension;
+    cattr.val.clusterDim.x = (unsigned)ncl;
+    cattr.val.clusterDim.y = 1;
+    cattr.val.clusterDim.z = 1;
+    cudaLaunchConfig_t ncfg;
+    std::memset(&ncfg, 0, sizeof(ncfg));
+    ncfg.gridDim = dim3((unsigned)ncl);
+    ncfg.blockDim = dim3(kNarrowBlock);
+    ncfg.dynamicSmemBytes = kNarrowSmem;
+    ncfg.stream = s;
+    ncfg.attrs = &cattr;
+    ncfg.numAttrs = ncl > 1 ? 1 : 0;
+    GRUS_CUDA_TRY(cudaLaunchKernelEx(&ncfg, bfs_narrow, a));
+  }
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev1, s));
   if (!dev_out) GRUS_CUDA_TRY(cudaMemcpyAsync(depth, w->depth, g->n * 4, cudaMemcpyDeviceToHost, s));
   if (!sync) return GRUS_OK;

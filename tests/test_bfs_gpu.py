@@ -157,13 +157,13 @@ def _broom(path_len, leaves):
 
 def test_bfs_long_tail_wide_vertex_and_spill(grus, oracle_mod):
     """A traversal past the hand-over level with a small frontier finishes in
-    the single-CTA tail; there the edges of a vertex of degree 10,000 are
-    dealt to all of the CTA's threads and its 10,000 neighbours overflow the
-    shared-memory frontier into the spill list.  Depths and counts equal the
-    oracle's."""
-    offs, cols = _broom(200, 10000)
+    the tail cluster; there the edges of a vertex of degree 100,001 are dealt
+    to all the threads of its owner CTA and its 100,000 neighbours overflow
+    the shared-memory frontiers (16 x 4,096 entries at most) into the spill
+    list.  Depths and counts equal the oracle's."""
+    offs, cols = _broom(200, 100000)
     g = grus.Graph.from_csr(offs, cols, symmetric=True)
-    _check_bfs(grus, oracle_mod, g, [0, 150, 199, 200 + 10000 + 5])
+    _check_bfs(grus, oracle_mod, g, [0, 150, 199, 200 + 100000 + 5])
 
 
 def test_bfs_long_tail_with_sinks(grus, oracle_mod):
