@@ -36,6 +36,7 @@ constexpr int kBlock = 256;
 constexpr uint32_t kCtaTh = 1024;   // in-degree from which a vertex is "heavy"
 constexpr uint32_t kHChunk = 2048;  // edges per heavy-vertex piece
 constexpr uint32_t kKahanTh = 16;
+constexpr int kShortSteps = 2;      // short-list steps whose gathers are in flight together
 
 struct Args {
   const uint32_t *__restrict__ toffs;  // CSC offsets
@@ -121,7 +122,40 @@ __device__ __forceinline__ float gather_seq(const Args &a, const float *cs, uint
 // lane k of a step takes edge k of the concatenation (coalesced source-id
 // loads, every lane busy), a segmented warp scan sums each vertex's run
 // within the step (a fixed pairwise order), and the owning lane adds its
-// run's sum.  Returns the full sum for the calling lane's vertex.
+// run's sum.  Steps go in rounds of kShortSteps: all their source ids, then
+// all their contributions, are loaded before any is summed (kShortSteps
+// gathers in flight per lane).  Returns the full sum for the calling lane's
+// vertex.
+__device__ __forceinline__ uint32_t short_owner(uint32_t incl, uint32_t k) {
+  int j = 0;
+#pragma unroll
+  for (int step = 16; step >= 1; step >>= 1) {
+    const uint32_t pv = __shfl_sync(0xffffffffu, incl, j + step - 1);
+    if (pv <= k) j += step;
+  }
+  return (uint32_t)j;
+}
+
+// Adds to acc the calling lane's run within the step starting at k0, whose
+// lane value is v (edge k0 + lane's contribution, 0 past the end).
+__device__ __forceinline__ void short_step(KSum &acc, uint32_t lane, uint32_t k0, uint32_t oe,
+                                           uint32_t excl, uint32_t incl, float v) {
+  bool head = lane == 0 || k0 + lane == oe;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const float tv = __shfl_up_sync(0xffffffffu, v, o);
+    const bool th = __shfl_up_sync(0xffffffffu, head, o);
+    if ((int)lane >= o && !head) {
+      v += tv;
+      head = th;
+    }
+  }
+  // this lane's run within the step ends at min(incl, k0 + 32) - 1
+  const uint32_t rs = max(excl, k0), re = min(incl, k0 + 32);
+  const float t = __shfl_sync(0xffffffffu, v, rs < re ? re - 1 - k0 : 0);
+  if (rs < re) acc.add(t);
+}
+
 __device__ __forceinline__ float gather_short(const Args &a, const float *cs, uint32_t beg,
                                               uint32_t deg) {
   const uint32_t lane = lane_id();
@@ -134,31 +168,23 @@ __device__ __forceinline__ float gather_short(const Args &a, const float *cs, ui
   const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
   const uint32_t excl = incl - deg;
   KSum acc;
-  for (uint32_t k0 = 0; k0 < total; k0 += 32) {
-    const uint32_t k = k0 + lane;
-    int j = 0;
+  constexpr int P = kShortSteps;
+  for (uint32_t k0 = 0; k0 < total; k0 += 32 * P) {
+    uint32_t oe[P], u[P];
+    float v[P];
 #pragma unroll
-    for (int step = 16; step >= 1; step >>= 1) {
-      const uint32_t pv = __shfl_sync(0xffffffffu, incl, j + step - 1);
-      if (pv <= k) j += step;
+    for (int i = 0; i < P; ++i) {
+      const uint32_t k = k0 + 32 * i + lane;
+      const uint32_t j = short_owner(incl, k);
+      const uint32_t ob = __shfl_sync(0xffffffffu, beg, j);
+      oe[i] = __shfl_sync(0xffffffffu, excl, j);
+      u[i] = k < total ? __ldg(a.tcols + ob + (k - oe[i])) : 0u;
     }
-    const uint32_t ob = __shfl_sync(0xffffffffu, beg, j);
-    const uint32_t oe = __shfl_sync(0xffffffffu, excl, j);
-    float v = k < total ? __ldcg(cs + __ldg(a.tcols + ob + (k - oe))) : 0.f;
-    bool head = lane == 0 || k == oe;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const float tv = __shfl_up_sync(0xffffffffu, v, o);
-      const bool th = __shfl_up_sync(0xffffffffu, head, o);
-      if ((int)lane >= o && !head) {
-        v += tv;
-        head = th;
-      }
-    }
-    // this lane's run within the step ends at min(incl, k0 + 32) - 1
-    const uint32_t rs = max(excl, k0), re = min(incl, k0 + 32);
-    const float t = __shfl_sync(0xffffffffu, v, rs < re ? re - 1 - k0 : 0);
-    if (rs < re) acc.add(t);
+    for (int i = 0; i < P; ++i) v[i] = k0 + 32 * i + lane < total ? __ldcg(cs + u[i]) : 0.f;
+#pragma unroll
+    for (int i = 0; i < P; ++i)
+      if (k0 + 32 * i < total) short_step(acc, lane, k0 + 32 * i, oe[i], excl, incl, v[i]);
   }
   return acc.value();
 }
@@ -175,7 +201,7 @@ __device__ __forceinline__ float gather_short(const Args &a, const float *cs, ui
 //   -- grid barrier --
 // so no block barrier separates the warps of a light tile, and a heavy
 // vertex is spread over many CTAs.  The heavy lists are built once per call.
-__global__ void __launch_bounds__(kBlock) pr_persistent(Args a) {
+__global__ void __launch_bounds__(kBlock, 8) pr_persistent(Args a) {
   __shared__ float s_part[kBlock / 32];
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
