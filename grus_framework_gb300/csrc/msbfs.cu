@@ -111,7 +111,7 @@ struct PushVisitor {
   }
 };
 
-__global__ void __launch_bounds__(kBlock) msbfs_persistent(Args a) {
+__global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
   const uint32_t lane = lane_id();
