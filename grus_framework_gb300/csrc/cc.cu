@@ -5,21 +5,26 @@
 // along every edge (:69-79), one kernel + compaction + host sync per round,
 // about diameter-many rounds.  On a symmetric graph its fixpoint is the minimum
 // vertex id of each component; this file computes the same labels with a
-// lock-free union-find whose link step always hooks the larger root under the
-// smaller one (so every root is the minimum of its set), organised as in
-// Afforest (Sutton, Ben-Nun & Barak, IPDPS 2018):
+// lock-free union-find organised as in Afforest (Sutton, Ben-Nun & Barak,
+// IPDPS 2018):
 //   1. parent[v] = v
-//   2. link every vertex with its first `kSample` neighbours, compress
+//   2. link every vertex with its first `kSample` neighbours (one pass), compress
 //   3. find the most frequent root among 1024 sampled vertices (the giant
 //      component) on the device
 //   4. every vertex outside the giant component links its remaining
 //      neighbours -- degree-binned with the mappings of expand.cuh; vertices
 //      inside it are skipped, their edges are seen from the other endpoint
-//   5. label[v] = find(v)
-// Labels are order-independent (the minimum of each set), so the result is
-// bit-exact against the oracle's union-find.  Edges are taken as undirected:
-// on a non-symmetric graph the result is its weakly connected components
-// (step 4 then skips nothing).
+//   5. label[v] = the smallest vertex id among the vertices with v's root
+// Linking hooks the root of lower priority under the root of higher
+// priority, priority = (degree, id): a hub becomes the root of its
+// neighbours' trees, so the many threads that link a low-degree vertex to
+// the same hub each swing their own root's parent instead of all racing for
+// the hub's (hooking by id made those threads retry one after another).
+// The root is then not the smallest id of its set, so step 5 takes the
+// minimum explicitly.  Labels are order-independent (the minimum of each
+// set), so the result is bit-exact against the oracle's union-find.  Edges
+// are taken as undirected: on a non-symmetric graph the result is its weakly
+// connected components (step 4 then skips nothing).
 #include <algorithm>
 #include <cstring>
 
@@ -46,15 +51,22 @@ __device__ __forceinline__ uint32_t find_root(uint32_t *p, uint32_t x) {
   return x;
 }
 
-__device__ __forceinline__ void link(uint32_t *p, uint32_t u, uint32_t v) {
+// Hooking priority of a vertex: its degree, ties broken by id (a total order,
+// so concurrent hooks never form a cycle).
+__device__ __forceinline__ uint64_t prio(const uint32_t *__restrict__ offs, uint32_t x) {
+  return ((uint64_t)(__ldg(offs + x + 1) - __ldg(offs + x)) << 32) | x;
+}
+
+__device__ __forceinline__ void link(const uint32_t *__restrict__ offs, uint32_t *p, uint32_t u,
+                                     uint32_t v) {
   uint32_t ru = find_root(p, u), rv = find_root(p, v);
   while (ru != rv) {
-    if (ru < rv) {
+    if (prio(offs, ru) > prio(offs, rv)) {
       const uint32_t t = ru;
       ru = rv;
       rv = t;
     }
-    const uint32_t old = atomicCAS(p + ru, ru, rv);  // hook larger root under smaller
+    const uint32_t old = atomicCAS(p + ru, ru, rv);  // hook lower priority under higher
     if (old == ru) return;
     ru = find_root(p, old);
     rv = find_root(p, rv);
@@ -66,20 +78,51 @@ __global__ void k_init(uint32_t *p, uint32_t n) {
     p[v] = v;
 }
 
+// Links every vertex with its first kSample neighbours in one pass: their
+// ids are loaded together (usually one line), then linked in turn.
 __global__ void k_link_sample(const uint32_t *__restrict__ offs, const uint32_t *__restrict__ cols,
-                              uint32_t *p, uint32_t n, uint32_t r) {
+                              uint32_t *p, uint32_t n) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     const uint32_t b = __ldg(offs + v), e = __ldg(offs + v + 1);
-    if (b + r < e) link(p, v, __ldg(cols + b + r));
+    uint32_t u[kSample];
+#pragma unroll
+    for (uint32_t r = 0; r < kSample; ++r) u[r] = b + r < e ? __ldg(cols + b + r) : v;
+#pragma unroll
+    for (uint32_t r = 0; r < kSample; ++r)
+      if (u[r] != v) link(offs, p, v, u[r]);
   }
 }
 
-__global__ void k_compress(uint32_t *p, uint32_t *out, uint32_t n) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-    const uint32_t r = find_root(p, v);
-    if (out) out[v] = r;
-    else p[v] = r;
+__global__ void k_compress(uint32_t *p, uint32_t n) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    p[v] = find_root(p, v);
+}
+
+// After a full compression (p[v] = root): lo[root] = the smallest member id.
+// lo starts at all ones.  A warp's lanes hold consecutive ids, so among the
+// lanes with the same root the lowest holds the smallest id and alone issues
+// the atomic, and only if its id is below the value it reads -- the giant
+// component costs a few atomics instead of one per member.
+__global__ void k_min_member(const uint32_t *__restrict__ p, uint32_t *lo, uint32_t n) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t v0 = blockIdx.x * blockDim.x; v0 < n; v0 += stride) {
+    const uint32_t v = v0 + threadIdx.x;
+    const uint32_t r = v < n ? __ldg(p + v) : 0xFFFFFFFFu;
+    const uint32_t peers = __match_any_sync(0xffffffffu, r);
+    const bool first = (peers & ((1u << (threadIdx.x & 31u)) - 1u)) == 0u;
+    if (v < n && first && v < lo[r]) atomicMin(lo + r, v);  // a stale read only costs an atomic
   }
+}
+
+__global__ void k_label(const uint32_t *__restrict__ p, const uint32_t *__restrict__ lo,
+                        uint32_t *label, uint32_t n) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    label[v] = __ldcg(lo + __ldg(p + v));
+}
+
+__global__ void k_fill(uint32_t *x, uint32_t val, uint32_t n) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    x[v] = val;
 }
 
 // Most frequent root among kModeSamples vertices picked by a fixed hash.
@@ -126,7 +169,7 @@ struct LinkVisitor {
   __device__ __forceinline__ uint32_t aux(uint32_t v) const { return __ldg(offs + v) + kSample; }
   __device__ __forceinline__ void edge(uint32_t src, uint32_t first, uint32_t x) {
     if (x < first) return;  // neighbours linked in the sampling rounds
-    link(p, src, __ldg(cols + x));
+    link(offs, p, src, __ldg(cols + x));
   }
 };
 
@@ -142,6 +185,7 @@ __global__ void __launch_bounds__(kBlock) k_link_rest(const uint32_t *__restrict
 
 struct Workspace {
   uint32_t *parent = nullptr, *queue = nullptr;
+  uint32_t *label = nullptr;  // labels for a host output buffer
   uint4 *chunks = nullptr;
   uint32_t ccap = 0;
   Ctl *ctl = nullptr, *ctl_host = nullptr;
@@ -153,6 +197,7 @@ void ws_free(void *q) {
   if (!w) return;
   cudaFree(w->parent);
   cudaFree(w->queue);
+  cudaFree(w->label);
   cudaFree(w->chunks);
   cudaFree(w->ctl);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -203,6 +248,7 @@ extern "C" int grus_cc(grus_graph *g, uint32_t *label, grus_stats *stats, void *
   int rc = ws_get(g, &w);
   if (rc) return rc;
   const bool dev_out = is_device_pointer(label);
+  if (!dev_out && !w->label) GRUS_CUDA_TRY(cudaMalloc(&w->label, g->n * 4));
   const uint32_t n = (uint32_t)g->n;
   const int sms = std::max(device_sm_count(), 1);
   const int grid = sms * 8;
@@ -212,16 +258,19 @@ extern "C" int grus_cc(grus_graph *g, uint32_t *label, grus_stats *stats, void *
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
   GRUS_CUDA_TRY(cudaMemsetAsync(w->ctl, 0, sizeof(Ctl), s));
   k_init<<<grid, kBlock, 0, s>>>(w->parent, n);
-  for (uint32_t r = 0; r < kSample; ++r)
-    k_link_sample<<<grid, kBlock, 0, s>>>(g->csr.offs, g->csr.cols, w->parent, n, r);
-  k_compress<<<grid, kBlock, 0, s>>>(w->parent, nullptr, n);
+  k_link_sample<<<grid, kBlock, 0, s>>>(g->csr.offs, g->csr.cols, w->parent, n);
+  k_compress<<<grid, kBlock, 0, s>>>(w->parent, n);
   k_giant<<<1, kModeSamples, 0, s>>>(w->parent, n, &w->ctl->giant);
   k_collect<<<grid, kBlock, 0, s>>>(g->csr.offs, w->parent, n, w->ctl, w->queue, w->chunks,
                                     w->ccap, huge, (g->flags & GRUS_GRAPH_SYMMETRIC) != 0);
   k_link_rest<<<sms * std::max(occ, 1), kBlock, 0, s>>>(g->csr.offs, g->csr.cols, w->parent,
                                                           w->ctl, w->queue, n, w->chunks, w->ccap);
-  uint32_t *dst = dev_out ? label : w->parent;
-  k_compress<<<grid, kBlock, 0, s>>>(w->parent, dev_out ? label : nullptr, n);
+  // canonical labels: the smallest member of each set (the queue is free now)
+  uint32_t *dst = dev_out ? label : w->label;
+  k_compress<<<grid, kBlock, 0, s>>>(w->parent, n);
+  k_fill<<<grid, kBlock, 0, s>>>(w->queue, 0xFFFFFFFFu, n);
+  k_min_member<<<grid, kBlock, 0, s>>>(w->parent, w->queue, n);
+  k_label<<<grid, kBlock, 0, s>>>(w->parent, w->queue, dst, n);
   GRUS_CUDA_TRY(cudaGetLastError());
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev1, s));
   if (!dev_out) GRUS_CUDA_TRY(cudaMemcpyAsync(label, dst, g->n * 4, cudaMemcpyDeviceToHost, s));
@@ -232,7 +281,7 @@ extern "C" int grus_cc(grus_graph *g, uint32_t *label, grus_stats *stats, void *
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
     stats->levels = kSample + 1;
-    stats->kernel_launches = 6 + kSample;
+    stats->kernel_launches = 10;
     stats->vertices_reached = g->n;
     stats->edges_reached = g->m;
     float ms = 0.f;
