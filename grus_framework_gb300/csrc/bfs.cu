@@ -57,7 +57,7 @@ namespace cg = cooperative_groups;
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 constexpr uint32_t kDefHuge = 8192;   // chunking threshold
-constexpr uint32_t kDefBuScan = 8;    // pull: neighbours a lane checks alone
+constexpr uint32_t kDefBuScan = 4;    // pull: neighbours a lane checks alone (one round)
 constexpr uint32_t kDefBuWords = 4;   // pull: bitmap words per warp step
 constexpr float kDefAlpha = 15.f, kDefBeta = 18.f;
 // Narrow tail: a traversal still running after kNarrowAfter levels, with a
