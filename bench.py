@@ -252,9 +252,10 @@ def msbfs_sources(n, offs_or_degree_fn, k, seed):
 
 # ---------------------------------------------------------------------------
 # CPU path (the oracle's OpenMP versions; bounded samples)
-def cpu_run(w, csr, csc, src, srcs, threads, budget_s=12.0, max_runs=5):
+def cpu_run(w, csr, csc, src, srcs, threads, budget_s=12.0, max_runs=5, nsrc=4):
     """Times the OpenMP version of the workload's algorithm on `threads` host
-    threads.  Returns (units per second, sample description)."""
+    threads (multi-source workloads: one run from each of the first `nsrc`
+    sources).  Returns (units per second, sample description)."""
     import oracle
     algo = w["algo"]
     times, units = [], 0
@@ -283,13 +284,13 @@ def cpu_run(w, csr, csc, src, srcs, threads, budget_s=12.0, max_runs=5):
     elif algo in ("msbfs", "msssp"):
         fn = oracle.omp_bfs if algo == "msbfs" else oracle.omp_sssp
         per = []
-        for s in srcs[:4]:  # bounded sample: 4 of the sources, one run each
+        for s in srcs[:nsrc]:  # bounded sample: nsrc of the sources, one run each
             d, t = fn(csr, int(s), threads)
             per.append((oracle.reached_edges(csr, d), t))
         units = sum(p[0] for p in per)
         times = [sum(p[1] for p in per)]
-        desc = (f"one OpenMP {'BFS' if algo == 'msbfs' else 'SSSP'} from each of the first 4 "
-                f"of the {len(srcs)} sources")
+        desc = (f"one OpenMP {'BFS' if algo == 'msbfs' else 'SSSP'} from each of the first "
+                f"{min(nsrc, len(srcs))} of the {len(srcs)} sources")
     med = statistics.median(times)
     return units / med / 1e9, f"{desc}, median {med*1e3:.1f} ms, OpenMP level-synchronous"
 
@@ -374,18 +375,25 @@ def run_grus(args, dist, rank, local):
     torch.cuda.synchronize()
     barrier(dist)
 
+    # Each step's time is the pair of CUDA events the C ABI records on the
+    # launching stream right before its first and after its last kernel
+    # (stats["device_ms"]), so host work between a step's flush and its launch
+    # (Python, ctypes) is not counted as device time; the events of this loop
+    # around each call are kept as a cross-check that does include it.
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
+    step_ms = []
     with ClockSampler(local) as clk:
         for i in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
             ev[i][0].record(stream)
-            call(out_dev)
+            _, st_i = call(out_dev, stats=True)
             ev[i][1].record(stream)
+            step_ms.append(st_i["device_ms"])
         torch.cuda.synchronize()
     barrier(dist)
-    step_ms = [a.elapsed_time(b) for a, b in ev]
+    outer_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = reduce_max(dist, sum(step_ms))
     ws = dist.get_world_size() if dist else 1
     total_units = reduce_sum(dist, units * args.steps)
@@ -446,6 +454,13 @@ def run_grus(args, dist, rank, local):
             v, sample = cpu_run(w, csr, csc, src, srcs, threads)
             cpu = {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": sample}
+            # the same port on one thread, one run (one source for multi-source;
+            # skipped above 2^30 edges, where it would take minutes)
+            if csr.m <= (1 << 30):
+                v1, sample1 = cpu_run(w, csr, csc, src, srcs, 1, budget_s=0.0, max_runs=1,
+                                      nsrc=1)
+                cpu["single_thread"] = {"value": round(v1, 4), "unit": UNIT, "cores": 1,
+                                        "sample": sample1}
         clocks = clk.summary()
         cfg = {k_: v_ for k_, v_ in w.items() if k_ not in ("metric", "kernel")}
         cfg.update({"n": n, "m": m, "src": src if algo not in ("msbfs", "msssp") else f"{k} seeded (seed 4)",
@@ -456,6 +471,7 @@ def run_grus(args, dist, rank, local):
         result = {
             "metric": w["metric"], "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(mean_ms, 4),
+            "ms_per_step_outer_events": round(sum(outer_ms) / len(outer_ms), 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if algo == "pagerank" else "u32",
             "data": "synthetic (generated on device from the seed)",
