@@ -181,7 +181,9 @@ int ws_get(grus_graph *g, Workspace **out) {
   w->W = (uint32_t)((g->n + 31) / 32);
   const uint64_t Wp = ((uint64_t)w->W + 31) / 32 * 32;  // 128-byte aligned maps
   w->bitmap_bytes = 4 * Wp * 4;
-  const uint32_t huge = tune_or(g->tuning.huge_degree, kDefHuge);
+  // chunk lists sized for any chunking degree down to 256 (the autotuner and
+  // callers may lower it after the workspace exists)
+  const uint32_t huge = std::min(tune_or(g->tuning.huge_degree, kDefHuge), 256u);
   const uint64_t cap = g->m / kChunk + g->m / std::max(huge, 1u) + 2;
   w->chunk_cap = (uint32_t)std::min<uint64_t>(cap, 0x7FFFFFFFull);
   cudaError_t e = cudaMalloc(&w->bitmaps, w->bitmap_bytes);

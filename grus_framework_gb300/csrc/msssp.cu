@@ -18,7 +18,7 @@ namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr uint32_t kDefDelta = 384;
+constexpr uint32_t kDefDelta = 640;
 constexpr int kMaxSources = 32;
 using ms::kPiece;
 using ms::Slot;

@@ -34,8 +34,8 @@ namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr uint32_t kDefHuge = 256;
-constexpr uint32_t kDefDelta = 192;
+constexpr uint32_t kDefHuge = 1024;
+constexpr uint32_t kDefDelta = 640;
 
 struct Slot {
   uint32_t qcount, ccount;
@@ -128,7 +128,9 @@ int ws_get(grus_graph *g, Workspace **out) {
   w->W = (uint32_t)((g->n + 31) / 32);
   const uint64_t Wp = ((uint64_t)w->W + 31) / 32 * 32;
   w->bitmap_bytes = 3 * Wp * 4;
-  const uint32_t huge = tune_or(g->tuning.huge_degree, kDefHuge);
+  // chunk lists sized for any chunking degree down to 256 (the autotuner and
+  // callers may lower it after the workspace exists)
+  const uint32_t huge = std::min(tune_or(g->tuning.huge_degree, kDefHuge), 256u);
   w->chunk_cap = (uint32_t)std::min<uint64_t>(g->m / kChunk + g->m / huge + 2, 0x7FFFFFFFull);
   const uint64_t n1 = std::max<uint64_t>(g->n, 1);
   cudaError_t e = cudaMalloc(&w->bitmaps, w->bitmap_bytes);

@@ -49,7 +49,7 @@ extern "C" int grus_autotune(grus_graph *g, uint32_t algo, uint32_t src, int rep
     knobs.push_back({&grus_tuning::huge_degree, nullptr, {512, 1024, 4096}});
     knobs.push_back({&grus_tuning::ctas_per_sm, nullptr, {0, 2, 3}});
   } else {
-    knobs.push_back({&grus_tuning::sssp_delta, nullptr, {16, 48, 96, 192, 512}});
+    knobs.push_back({&grus_tuning::sssp_delta, nullptr, {96, 192, 384, 640, 1024}});
     knobs.push_back({&grus_tuning::huge_degree, nullptr, {512, 1024, 4096}});
     knobs.push_back({&grus_tuning::ctas_per_sm, nullptr, {0, 2, 3}});
   }
