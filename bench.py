@@ -23,8 +23,15 @@ events.
 
 Other workloads (`--workload`): sssp-rmat22, cc-rmat22, pagerank-rmat24
 (directed), bfs-grid4096, bfs-rmat26-managed (managed memory, device budget
-half the CSR bytes), msbfs-rmat23 (64 sources), msssp-rmat22 (32 sources).  `--scale` overrides
-the RMAT scale (or the grid side as a power of two) for small profiling runs.
+half the CSR bytes), msbfs-rmat23 (64 sources), msssp-rmat22 (32 sources),
+and the two systems forms in queries/s: batch-c4b (256 SSSP queries over 32
+resident RMAT graphs of scales 14-20 in one batched call per step; also the
+same queries as back-to-back plain calls) and serve-c5 (Poisson arrivals at
+8,000 queries/s against 8 resident RMAT graphs of scales 16-24, half SSSP,
+through the query server; a step is 1,000 queries; p50/p99 latency, a sweep
+of lower arrival rates, and back-to-back plain calls of the same mix).
+`--scale` overrides the RMAT scale (or the grid side as a power of two) for
+small profiling runs.
 
 `--impl reference` times the CPU path (the reference has no host traversal;
 the plain OpenMP version of the same algorithm in the oracle stands in) on
@@ -52,6 +59,34 @@ FALLBACK_HBM_GBS = 6800.0
 UNIT = "GTEPS"
 INFINIT = 4294967294
 
+# Graph sets of the batched (C4b) and served (C5) workloads: (scale, edge
+# factor, generator seed), symmetrised, weighted, relabelled.
+def batch_graph_specs(seed):
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(32):
+        sc = int(rng.integers(14, 21))
+        ef = int(rng.choice([8, 16, 32]))
+        specs.append((sc, ef, 900 + i))
+    return specs, rng
+
+
+SERVE_SCALES = [16, 17, 18, 19, 20, 21, 22, 24]
+
+
+def serve_graph_specs():
+    return [(s, 16, 50 + s) for s in SERVE_SCALES]
+
+
+def draw_source(rng, offs):
+    """A random vertex of degree > 0 (the rule for multi-source and served queries)."""
+    n = len(offs) - 1
+    while True:
+        v = int(rng.integers(n))
+        if offs[v + 1] > offs[v]:
+            return v
+
+
 WORKLOADS = {
     "bfs-rmat24": dict(algo="bfs", graph="rmat", scale=24, edge_factor=16, seed=3,
                        symmetric=True, weighted=False, kernel="bfs_persistent",
@@ -76,6 +111,15 @@ WORKLOADS = {
                                managed=True, budget_fraction=0.5,
                                metric="GTEPS (single-query BFS, RMAT-26 symmetrised, managed "
                                       "memory, device budget 50% of the CSR bytes)"),
+    "batch-c4b": dict(algo="batch", graph="rmat-set", seed=4, queries=256, kernel="batch_kernel "
+                      "(cluster workers) + msssp_persistent (graphs of 2^23+ edges)",
+                      metric="queries/s (256 SSSP queries over 32 resident RMAT graphs, scales "
+                             "14-20, edge factors 8-32, one batched call)"),
+    "serve-c5": dict(algo="serve", graph="rmat-set", seed=5, rate=8000, sweep_rates=[500, 2000],
+                     sweep_queries=2000, step_queries=1000, sssp_fraction=0.5,
+                     kernel="server lanes: batch_kernel slots + whole-GPU bfs/sssp/msssp launches",
+                     metric="queries/s served (Poisson arrivals at 8,000/s, 8 resident RMAT graphs "
+                            "s16-24, half SSSP), p50/p99 latency"),
     "msssp-rmat22": dict(algo="msssp", graph="rmat", scale=22, edge_factor=16, seed=2,
                          symmetric=True, weighted=True, kernel="msssp_persistent", sources=32,
                          metric="GTEPS (32-source SSSP in one launch, RMAT-22 symmetrised, w in [1,255])"),
@@ -493,6 +537,377 @@ def run_grus(args, dist, rank, local):
     return result
 
 
+# ---------------------------------------------------------------------------
+# batched (C4b) and served (C5) forms
+QPS = "queries/s"
+
+
+def sssp_or_bfs_bytes(algo_id, n, deg, d):
+    """Algorithmic bytes of one BFS (algo 0) or SSSP (algo 1) query from its result."""
+    reached = d != INFINIT
+    nr = int(np.count_nonzero(reached))
+    mr = int(deg[reached].sum())
+    return alg_bytes("sssp" if algo_id == 1 else "bfs", n, 0, nr, mr)
+
+
+def cpu_queries(graphs_host, queries, threads):
+    """OpenMP BFS/SSSP of `queries` ((graph, algo, src) tuples) on host CSRs.
+    Returns (queries per second, total seconds)."""
+    import oracle
+    total = 0.0
+    for gi, algo_id, src in queries:
+        fn = oracle.omp_sssp if algo_id == 1 else oracle.omp_bfs
+        total += fn(graphs_host[gi], int(src), threads)[1]
+    return len(queries) / total, total
+
+
+def roofline_entry(alg, seconds, traffic_key, kernel, note=None):
+    peak, peak_kind = measured_peaks()
+    achieved = alg / seconds / 1e9
+    traffic, note = None, None
+    prof = ROOT / "profiles" / "dram_traffic.json"
+    if prof.exists():
+        rec = json.loads(prof.read_text()).get(traffic_key)
+        if rec:
+            traffic, note = rec.get("dram_bytes_per_launch"), rec.get("note")
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_note": note,
+            "peak_source": peak_kind, "kernel": kernel, "algorithmic_bytes_per_launch": alg,
+            **({"algorithmic_bytes_note": note} if note else {})}
+
+
+def run_batch(args, dist, rank, local):
+    """256 SSSP queries over 32 resident graphs in one batched call per step."""
+    import ctypes
+    import torch
+    import grus_framework_gb300 as grus
+
+    torch.cuda.set_device(local)
+    grus.device_init(local)
+    w = workload_spec(args)
+    specs, rng = batch_graph_specs(w["seed"])
+    gs = [grus.Graph.rmat(sc, ef, sd, symmetric=True, weighted=True, relabel=True)
+          for sc, ef, sd in specs]
+    offs = [g.copy_offsets() for g in gs]
+    degs = [np.diff(o.astype(np.int64)) for o in offs]
+    queries = []
+    for i in range(w["queries"]):
+        gi = i % len(gs)
+        queries.append((gi, grus.ALGO_SSSP, draw_source(rng, offs[gi])))
+    b = grus.Batch(gs)
+    layout, total = b.layout(queries)
+    out = torch.empty(total, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    st = b.run(queries, out, layout, use_graph=True, stats=True)
+    launches = max(int(st["kernel_launches"]), 1)
+    for _ in range(args.warmup):
+        b.run(queries, out, layout, use_graph=True)
+    torch.cuda.synchronize()
+    barrier(dist)
+    step_ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            step_ms.append(b.run(queries, out, layout, use_graph=True, stats=True)["device_ms"])
+        torch.cuda.synchronize()
+    barrier(dist)
+    nq = len(queries)
+    total_ms = reduce_max(dist, sum(step_ms))
+    value = reduce_sum(dist, nq * args.steps) / (total_ms * 1e-3)
+    mean_ms = sum(step_ms) / len(step_ms)
+
+    # end to end: the batched call plus every result copied to pinned host memory
+    out_host = torch.empty(total, dtype=torch.int32, pin_memory=True)
+    e2e_s = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run(queries, out, layout, use_graph=True)
+        out_host.copy_(out)
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_value = reduce_sum(dist, nq * args.steps) / reduce_max(dist, sum(e2e_s))
+    res = out_host.numpy().view(np.uint32)
+    alg = 0
+    for (gi, algo_id, src), off in zip(queries, layout):
+        d = res[off: off + gs[gi].n]
+        assert d[src] == 0
+        alg += sssp_or_bfs_bytes(algo_id, gs[gi].n, degs[gi], d)
+
+    # the comparison the batched form is for: the same queries as plain calls
+    outs = [torch.empty(g.n, dtype=torch.int32, device="cuda") for g in gs]
+    for gi, _, src in queries[:32]:
+        grus.sssp(gs[gi], src, out=outs[gi])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for gi, _, src in queries:
+        grus.sssp(gs[gi], src, out=outs[gi])
+    torch.cuda.synchronize()
+    plain_qps = nq / (time.perf_counter() - t0)
+
+    result = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            sample = queries[:16]
+            hosts = {}
+            for gi, _, _ in sample:
+                if gi not in hosts:
+                    import oracle
+                    o_, c_, wt_ = gs[gi].copy_csr()
+                    hosts[gi] = oracle.CSR(o_, c_, wt_)
+            threads = host_threads()
+            v, sec = cpu_queries(hosts, sample, threads)
+            v1, sec1 = cpu_queries(hosts, sample[:4], 1)
+            cpu = {"value": round(v, 2), "unit": QPS, "cores": threads, "kind": "port",
+                   "sample": f"OpenMP SSSP of the first {len(sample)} queries, {sec:.2f} s",
+                   "single_thread": {"value": round(v1, 2), "unit": QPS, "cores": 1,
+                                     "sample": f"the first 4 queries, {sec1:.2f} s"}}
+        info = b.info()
+        cfg = {"workload": w["workload"], "graphs": len(gs),
+               "graph_specs": "RMAT scale 14-20, edge factor 8/16/32 drawn with seed 4, "
+                              "generator seeds 900-931, symmetrised, w in [1,255]",
+               "queries": nq, "sources": "degree > 0, seed 4", "sum_n": int(sum(g.n for g in gs)),
+               "sum_m": int(sum(g.m for g in gs)), "workers": info["workers"],
+               "cluster_size": info["cluster_size"], "big_edges": info["big_edges"],
+               "l2": "flushed (256 MB write) before each step", "parallelism": f"replicas x{dist.get_world_size() if dist else 1}"}
+        result = {
+            "metric": w["metric"], "value": round(value, 1), "unit": QPS,
+            "n_gpus": dist.get_world_size() if dist else 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(mean_ms, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (generated on device from the seeds)", "config": cfg,
+            "e2e": {"value": round(e2e_value, 1), "unit": QPS,
+                    "h2d_bytes_per_step": nq * ctypes.sizeof(grus.Query),
+                    "d2h_bytes_per_step": int(total) * 4,
+                    "note": "batched call through the public API, every result copied to "
+                            "pinned host memory inside the timed region"},
+            "plain_back_to_back": {"value": round(plain_qps, 1), "unit": QPS,
+                                   "note": "the same 256 queries as plain grus_sssp calls, "
+                                           "device outputs, host clock"},
+            "gpu_launches": launches * args.steps,
+            "roofline": roofline_entry(alg, mean_ms * 1e-3, w["workload"], w["kernel"]),
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+        }
+    b.free()
+    return result
+
+
+def serve_stream(srv, grus, gs, qo, rng, offs, rate, nq, frac, copy=None):
+    """Submits nq queries at Poisson arrivals of `rate` per second and polls
+    their completions.  Returns (seconds, latencies in us, errors, d2h bytes)."""
+    qs = []
+    for _ in range(nq):
+        gi = int(rng.integers(len(gs)))
+        algo_id = grus.ALGO_SSSP if rng.random() < frac else grus.ALGO_BFS
+        qs.append((gi, algo_id, draw_source(rng, offs[gi])))
+    arr = np.cumsum(rng.exponential(1.0 / rate, size=nq))
+    done = {}
+    d2h = 0
+    t0 = time.perf_counter()
+    i = 0
+    while len(done) < nq and time.perf_counter() - t0 < 300:
+        now = time.perf_counter() - t0
+        while i < nq and arr[i] <= now:
+            gi, algo_id, src = qs[i]
+            srv.submit(gi, algo_id, src, qo[gi][i % len(qo[gi])], i)
+            i += 1
+        comp = srv.poll(512, wait_ms=0 if i < nq else 1)
+        for tag, stt, lat in comp:
+            done[tag] = (stt, lat)
+            if copy is not None:
+                gi = qs[tag][0]
+                copy(gi, qo[gi][tag % len(qo[gi])])
+                d2h += gs[gi].n * 4
+    dt = time.perf_counter() - t0
+    lat = np.array([v[1] for v in done.values()])
+    errors = sum(1 for v in done.values() if v[0] != 0) + (nq - len(done))
+    return dt, lat, errors, d2h, len(done)
+
+
+def run_serve(args, dist, rank, local):
+    """Poisson query stream against 8 resident graphs through the server."""
+    import torch
+    import grus_framework_gb300 as grus
+
+    torch.cuda.set_device(local)
+    grus.device_init(local)
+    w = workload_spec(args)
+    gs = [grus.Graph.rmat(sc, ef, sd, symmetric=True, weighted=True, relabel=True)
+          for sc, ef, sd in serve_graph_specs()]
+    offs = [g.copy_offsets() for g in gs]
+    degs = [np.diff(o.astype(np.int64)) for o in offs]
+    rng = np.random.default_rng(w["seed"])
+    frac = w["sssp_fraction"]
+    # per-query algorithmic bytes of each (graph, algorithm), from one plain
+    # query per pair (random sources of degree > 0 reach the giant component)
+    per_q = {}
+    outs = [torch.empty(g.n, dtype=torch.int32, device="cuda") for g in gs]
+    for gi, g in enumerate(gs):
+        src = draw_source(rng, offs[gi])
+        for algo_id, fn in ((grus.ALGO_BFS, grus.bfs), (grus.ALGO_SSSP, grus.sssp)):
+            d = fn(g, src, out=outs[gi]).cpu().numpy().view(np.uint32)
+            per_q[(gi, algo_id)] = sssp_or_bfs_bytes(algo_id, g.n, degs[gi], d)
+    # plain back-to-back on 400 queries of the same mix
+    plain = []
+    for _ in range(400):
+        gi = int(rng.integers(len(gs)))
+        plain.append((gi, grus.ALGO_SSSP if rng.random() < frac else grus.ALGO_BFS,
+                      draw_source(rng, offs[gi])))
+    for gi, algo_id, src in plain[:16]:
+        (grus.sssp if algo_id else grus.bfs)(gs[gi], src, out=outs[gi])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for gi, algo_id, src in plain:
+        (grus.sssp if algo_id else grus.bfs)(gs[gi], src, out=outs[gi])
+        torch.cuda.synchronize()
+    plain_qps = len(plain) / (time.perf_counter() - t0)
+
+    qo = [[torch.empty(g.n, dtype=torch.int32, device="cuda") for _ in range(16)] for g in gs]
+    srv = grus.Server(gs)
+    for _ in range(args.warmup):
+        serve_stream(srv, grus, gs, qo, rng, offs, w["rate"], 200, frac)
+    torch.cuda.synchronize()
+    barrier(dist)
+    secs, lats, errors, completed = 0.0, [], 0, 0
+    st0 = srv.stats()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            dt, lat, err, _, nd = serve_stream(srv, grus, gs, qo, rng, offs, w["rate"],
+                                               w["step_queries"], frac)
+            secs += dt
+            lats.append(lat)
+            errors += err
+            completed += nd
+    barrier(dist)
+    st1 = srv.stats()
+    launches = st1["kernel_launches"] - st0["kernel_launches"]
+    lat_all = np.concatenate(lats)
+    value = reduce_sum(dist, completed) / reduce_max(dist, secs)
+    # end to end: every completed result copied to pinned host memory as it completes
+    host = [torch.empty(g.n, dtype=torch.int32, pin_memory=True) for g in gs]
+    cs = torch.cuda.Stream()
+
+    def copy(gi, buf):
+        with torch.cuda.stream(cs):
+            host[gi].copy_(buf, non_blocking=True)
+
+    e_secs, e_done, e_d2h = 0.0, 0, 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, err, d2h, nd = serve_stream(srv, grus, gs, qo, rng, offs, w["rate"],
+                                          w["step_queries"], frac, copy=copy)
+        cs.synchronize()
+        e_secs += time.perf_counter() - t0
+        e_done += nd
+        e_d2h += d2h
+        errors += err
+    e2e_value = reduce_sum(dist, e_done) / reduce_max(dist, e_secs)
+    sweep = []
+    for rate in w["sweep_rates"]:
+        dt, lat, err, _, nd = serve_stream(srv, grus, gs, qo, rng, offs, rate,
+                                           w["sweep_queries"], frac)
+        sweep.append({"offered_per_s": rate, "queries": int(nd), "queries_per_s": round(nd / dt, 1),
+                      "p50_ms": round(float(np.percentile(lat, 50)) / 1e3, 3),
+                      "p99_ms": round(float(np.percentile(lat, 99)) / 1e3, 3), "errors": int(err)})
+        errors += err
+    srv.close()
+    # algorithmic bytes of the timed queries: the mean per-query figure of the mix
+    mean_q = sum((frac if a == grus.ALGO_SSSP else 1 - frac) * v / len(gs)
+                 for (gi, a), v in per_q.items())
+    result = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            import oracle
+            sample = plain[:12]
+            hosts = {}
+            for gi, _, _ in sample:
+                if gi not in hosts:
+                    o_, c_, wt_ = gs[gi].copy_csr()
+                    hosts[gi] = oracle.CSR(o_, c_, wt_)
+            threads = host_threads()
+            v, sec = cpu_queries(hosts, sample, threads)
+            cpu = {"value": round(v, 2), "unit": QPS, "cores": threads, "kind": "port",
+                   "sample": f"OpenMP BFS/SSSP of {len(sample)} queries of the mix, {sec:.2f} s"}
+        cfg = {"workload": w["workload"], "graphs": "RMAT scales 16-22 and 24, edge factor 16, "
+                                                     "seeds 50+scale, symmetrised, w in [1,255]",
+               "offered_per_s": w["rate"], "queries": int(completed), "sssp_fraction": frac,
+               "sources": "degree > 0, seed 5", "server": "16 slots of 8-CTA workers, whole-GPU "
+               "lane for graphs of 2^20+ edges",
+               "big_launches": int(st1["big_launches"] - st0["big_launches"]),
+               "big_queries": int(st1["big_queries"] - st0["big_queries"]), "errors": int(errors),
+               "parallelism": f"replicas x{dist.get_world_size() if dist else 1}"}
+        result = {
+            "metric": w["metric"], "value": round(value, 1), "unit": QPS,
+            "n_gpus": dist.get_world_size() if dist else 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(secs / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (generated on device from the seeds)", "config": cfg,
+            "latency": {"p50_ms": round(float(np.percentile(lat_all, 50)) / 1e3, 3),
+                        "p99_ms": round(float(np.percentile(lat_all, 99)) / 1e3, 3),
+                        "measured": "submission to completion, per query, host clock"},
+            "sweep": sweep,
+            "e2e": {"value": round(e2e_value, 1), "unit": QPS, "h2d_bytes_per_step": 16 * w["step_queries"],
+                    "d2h_bytes_per_step": int(e_d2h / max(args.steps, 1)),
+                    "note": "the same stream with every result copied to pinned host memory as "
+                            "it completes"},
+            "plain_back_to_back": {"value": round(plain_qps, 1), "unit": QPS,
+                                   "note": "400 queries of the same mix as plain calls, one at a "
+                                           "time, host clock"},
+            "gpu_launches": int(launches),
+            "roofline": roofline_entry(int(mean_q * completed), secs, w["workload"], w["kernel"],
+                                       note="all queries of the timed region: per query the "
+                                            "BFS/SSSP figure of its graph, averaged over the mix"),
+            "cpu_baseline": cpu, "clocks": clk.summary(),
+        }
+    return result
+
+
+
+def run_reference_queries(args, w):
+    """CPU path of the batched / served workloads: the same graphs generated on
+    the host, the same queries, each step a bounded sample of them through the
+    OpenMP port on all host cores (queries per second)."""
+    import oracle
+    flags = oracle.GEN_SYMMETRIC | oracle.GEN_WEIGHTED | oracle.GEN_RELABEL
+    if w["algo"] == "batch":
+        specs, rng = batch_graph_specs(w["seed"])
+        hosts = [oracle.rmat(sc, ef, sd, flags) for sc, ef, sd in specs]
+        queries = [(i % len(hosts), 1, draw_source(rng, hosts[i % len(hosts)].offs))
+                   for i in range(w["queries"])]
+        per_step = 8
+    else:
+        hosts = [oracle.rmat(sc, ef, sd, flags) for sc, ef, sd in serve_graph_specs()]
+        rng = np.random.default_rng(w["seed"])
+        queries = []
+        for _ in range(400):
+            gi = int(rng.integers(len(hosts)))
+            queries.append((gi, 1 if rng.random() < w["sssp_fraction"] else 0,
+                            draw_source(rng, hosts[gi].offs)))
+        per_step = 6
+    threads = host_threads()
+    for k in range(max(args.warmup - 1, 0)):
+        cpu_queries(hosts, queries[:1], threads)
+    rates = []
+    for k in range(args.steps):
+        sample = [queries[(k * per_step + j) % len(queries)] for j in range(per_step)]
+        rates.append(cpu_queries(hosts, sample, threads)[0])
+    value = statistics.median(rates)
+    cfg = {"workload": w["workload"], "graphs": len(hosts), "queries_per_step": per_step,
+           "sum_n": int(sum(h.n for h in hosts)), "sum_m": int(sum(h.m for h in hosts))}
+    return {
+        "metric": w["metric"], "value": round(value, 2), "unit": QPS, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic (generated on the host from the seeds)",
+        "impl": "reference", "config": cfg,
+        "cpu_baseline": {"value": round(value, 2), "unit": QPS, "cores": threads, "kind": "port",
+                         "sample": f"each step: {per_step} of the queries, one OpenMP BFS/SSSP "
+                                   "each, back to back"},
+        "e2e": {"value": round(value, 2), "unit": QPS, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 def run_reference(args, dist, rank):
     """CPU path: the oracle's OpenMP version on the host cores (rank 0 only)."""
     if rank != 0:
@@ -500,6 +915,8 @@ def run_reference(args, dist, rank):
     import oracle
     w = workload_spec(args)
     algo = w["algo"]
+    if algo in ("batch", "serve"):
+        return run_reference_queries(args, w)
     g = host_graph(w)
     src = grid_source(1 << w["scale"]) if w["graph"] == "grid" else oracle.max_degree_vertex(g)
     csc = oracle.csr_to_csc(g) if algo == "pagerank" else None
@@ -543,8 +960,13 @@ def main():
         args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
     dist = init_dist(ws)
+    algo = WORKLOADS[args.workload]["algo"]
     if args.impl == "reference":
         res = run_reference(args, dist, rank)
+    elif algo == "batch":
+        res = run_batch(args, dist, rank, local)
+    elif algo == "serve":
+        res = run_serve(args, dist, rank, local)
     else:
         res = run_grus(args, dist, rank, local)
     if rank == 0 and res is not None:

@@ -97,7 +97,7 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
                 ("pending", C.c_uint64), ("rejected", C.c_uint64), ("slots", C.c_uint32),
                 ("slots_ready", C.c_uint32), ("big_launches", C.c_uint64),
-                ("big_queries", C.c_uint64)]
+                ("big_queries", C.c_uint64), ("kernel_launches", C.c_uint64)]
 
 
 class Telemetry(C.Structure):
@@ -367,6 +367,13 @@ class Graph:
                                        _ptr(wts) if wts is not None else None),
                "grus_graph_copy_csr")
         return offs, cols[: inf.m], (wts[: inf.m] if wts is not None else None)
+
+    def copy_offsets(self):
+        """The CSR offsets alone (n + 1 entries) on the host."""
+        offs = np.empty(self.info().n + 1, np.uint32)
+        _check(lib.grus_graph_copy_csr(self._handle(), _ptr(offs), None, None),
+               "grus_graph_copy_csr")
+        return offs
 
     def build_csc(self):
         _check(lib.grus_graph_build_csc(self._handle()), "grus_graph_build_csc")

@@ -82,6 +82,7 @@ struct grus_server {
   std::thread worker, big_worker;
   cudaStream_t big_stream = nullptr;
   uint64_t big_launches = 0, big_queries = 0;
+  std::atomic<uint64_t> kernel_launches{0};  // kernels launched for queries, both lanes
   std::atomic<bool> stop{false};
   int device = 0;
   uint64_t admitted = 0, finished = 0, rejected = 0;
@@ -124,6 +125,7 @@ int slot_launch(grus_server *s, Slot &sl, const Request &r) {
   int rc = batch_launch(sl.state, 0, 1, s->cluster, s->d_graphs, sl.d_task, 1, r.out, s->huge,
                         s->delta, sl.counter, sl.stream);
   if (rc) return rc;
+  s->kernel_launches += 1;
   GRUS_CUDA_TRY(cudaMemcpyAsync(sl.h_err, sl.state.err, 4, cudaMemcpyDeviceToHost, sl.stream));
   GRUS_CUDA_TRY(cudaMemsetAsync(sl.state.err, 0, 4, sl.stream));
   GRUS_CUDA_TRY(cudaEventRecord(sl.done, sl.stream));
@@ -278,6 +280,8 @@ int big_launch(grus_server *s, BigJob &j) {
              : msbfs_run(g, srcs, (int)j.group.size(), outs, nullptr, s->big_stream);
   }
   if (rc) return rc;
+  // a single BFS is the persistent kernel and its narrow-tail kernel
+  s->kernel_launches += (!multi && r.algo != GRUS_ALGO_SSSP) ? 2 : 1;
   j.ctrl = r.algo == GRUS_ALGO_SSSP ? (multi ? msssp_ctrl(g) : sssp_ctrl(g))
                                     : (multi ? msbfs_ctrl(g) : bfs_ctrl(g));
   *j.h_err = 0;
@@ -519,6 +523,7 @@ int grus_server_get_stats(grus_server *s, grus_server_stats *st) {
   st->completed = s->finished;
   st->big_launches = s->big_launches;
   st->big_queries = s->big_queries;
+  st->kernel_launches = s->kernel_launches.load();
   st->slots_ready = (uint32_t)s->slots_ready;
   st->rejected = s->rejected;
   st->slots = (uint32_t)s->slots.size();

@@ -375,6 +375,7 @@ typedef struct grus_server_stats {
   uint64_t big_launches;     /* whole-GPU launches of the big-graph lane */
   uint64_t big_queries;      /* queries they served (SSSP queries on one graph
                                 share a multi-source launch) */
+  uint64_t kernel_launches;  /* kernels launched for queries, both lanes */
 } grus_server_stats;
 
 GRUS_API int grus_server_create(grus_graph *const *graphs, int ngraphs,
