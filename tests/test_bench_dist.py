@@ -54,3 +54,24 @@ def test_reference_arm_under_torchrun_prints_one_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0
     assert d["cpu_baseline"]["cores"] >= 1 and d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_query_workload_helpers():
+    """The graph sets and source rule of the batched and served workloads are
+    deterministic, and the CPU rate of a query sample is positive."""
+    sys.path.insert(0, str(ROOT))
+    import numpy as np
+    import bench
+    import oracle
+    a, _ = bench.batch_graph_specs(4)
+    b, _ = bench.batch_graph_specs(4)
+    assert a == b and len(a) == 32
+    assert all(14 <= sc <= 20 and ef in (8, 16, 32) for sc, ef, _ in a)
+    assert [sc for sc, _, _ in bench.serve_graph_specs()] == [16, 17, 18, 19, 20, 21, 22, 24]
+    g = oracle.rmat(10, 8, 3, oracle.GEN_SYMMETRIC | oracle.GEN_WEIGHTED | oracle.GEN_RELABEL)
+    rng = np.random.default_rng(5)
+    srcs = [bench.draw_source(rng, g.offs) for _ in range(50)]
+    assert all(g.offs[v + 1] > g.offs[v] for v in srcs)
+    qps, sec = bench.cpu_queries({0: g}, [(0, 1, srcs[0]), (0, 0, srcs[1])], 2)
+    assert qps > 0 and sec > 0
+

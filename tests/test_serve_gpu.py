@@ -44,6 +44,7 @@ def test_server_results_same_alone_and_in_mix(grus, graphs):
         assert np.array_equal(out.cpu().numpy().view(np.uint32), alone)
     st = srv.stats()
     assert st["completed"] == len(reqs) and st["pending"] == 0 and st["slots_ready"] >= 1
+    assert st["kernel_launches"] >= len(reqs)  # at least one kernel per query
     srv.close()
 
 
@@ -92,6 +93,9 @@ def test_server_big_lane_groups_bfs_and_matches_alone(grus, graphs):
     st = srv.stats()
     assert st["big_queries"] == len(reqs) and st["completed"] == len(reqs)
     assert st["big_launches"] < len(reqs)  # queries were packed
+    # a BFS alone is two kernels (persistent kernel, narrow tail), a pack one
+    n_bfs = sum(1 for _, algo, _ in reqs if algo == grus.ALGO_BFS)
+    assert st["kernel_launches"] == st["big_launches"] + n_bfs
     srv.close()
 
 
