@@ -58,6 +58,9 @@ constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 constexpr uint32_t kDefHuge = 8192;   // chunking threshold
 constexpr uint32_t kDefBuScan = 4;    // pull: neighbours a lane checks alone (one round)
+// ... for a managed graph, whose adjacency may be read over the host link:
+// deferring fewer lists to the warp's 32-neighbour rounds reads fewer lines
+constexpr uint32_t kDefBuScanManaged = 8;
 constexpr uint32_t kDefBuWords = 4;   // pull: bitmap words per warp step
 constexpr float kDefAlpha = 15.f, kDefBeta = 18.f;
 // Narrow tail: a traversal still running after kNarrowAfter levels, with a
@@ -877,7 +880,8 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   a.alpha = tune_or(g->tuning.alpha, kDefAlpha);
   a.beta = tune_or(g->tuning.beta, kDefBeta);
   a.huge = tune_or(g->tuning.huge_degree, kDefHuge);
-  a.bu_scan = tune_or(g->tuning.bu_scan, kDefBuScan);
+  a.bu_scan = tune_or(g->tuning.bu_scan,
+                      g->mem_mode == GRUS_MEM_MANAGED ? kDefBuScanManaged : kDefBuScan);
   const int ncl = narrow_cluster();
   a.narrow_nf = kNarrowNf * (uint32_t)ncl;
   a.ho = (Handover *)(w->ctrl + kOffHandover);
