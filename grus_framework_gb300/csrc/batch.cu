@@ -389,8 +389,7 @@ int batch_occupancy(int cluster, int *workers) {
     const int rc = allow_wide_clusters();
     if (rc) return rc;
   }
-  cudaLaunchConfig_t cfg;
-  std::memset(&cfg, 0, sizeof(cfg));
+  cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeClusterDimension;
   attr.val.clusterDim.x = cluster;
@@ -521,8 +520,7 @@ int batch_launch(BatchState &st, int worker0, int nworkers, int cluster, const G
   attr.val.clusterDim.x = cluster;
   attr.val.clusterDim.y = 1;
   attr.val.clusterDim.z = 1;
-  cudaLaunchConfig_t cfg;
-  std::memset(&cfg, 0, sizeof(cfg));
+  cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(cluster * nworkers));
   cfg.blockDim = dim3(kBatchBlock);
   cfg.stream = s;

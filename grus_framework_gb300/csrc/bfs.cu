@@ -55,7 +55,6 @@ namespace {
 namespace cg = cooperative_groups;
 
 constexpr int kBlock = 256;
-constexpr int kWarps = kBlock / 32;
 constexpr uint32_t kDefHuge = 8192;   // chunking threshold
 constexpr uint32_t kDefBuScan = 4;    // pull: neighbours a lane checks alone (one round)
 // ... for a managed graph, whose adjacency may be read over the host link:
@@ -791,8 +790,7 @@ int narrow_cluster() {
       attr.val.clusterDim.x = (unsigned)k;
       attr.val.clusterDim.y = 1;
       attr.val.clusterDim.z = 1;
-      cudaLaunchConfig_t cfg;
-      std::memset(&cfg, 0, sizeof(cfg));
+      cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3((unsigned)k);
       cfg.blockDim = dim3(kNarrowBlock);
       cfg.dynamicSmemBytes = kNarrowSmem;
@@ -902,8 +900,7 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
     attrs[nattr].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     ++nattr;
   }
-  cudaLaunchConfig_t cfg;
-  std::memset(&cfg, 0, sizeof(cfg));
+  cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(sms * per_sm));
   cfg.blockDim = dim3(kBlock);
   cfg.dynamicSmemBytes = 0;
@@ -922,8 +919,7 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
     cattr.val.clusterDim.x = (unsigned)ncl;
     cattr.val.clusterDim.y = 1;
     cattr.val.clusterDim.z = 1;
-    cudaLaunchConfig_t ncfg;
-    std::memset(&ncfg, 0, sizeof(ncfg));
+    cudaLaunchConfig_t ncfg = {};
     ncfg.gridDim = dim3((unsigned)ncl);
     ncfg.blockDim = dim3(kNarrowBlock);
     ncfg.dynamicSmemBytes = kNarrowSmem;
@@ -1113,8 +1109,7 @@ extern "C" int grus_bfs_static(uint64_t n, uint64_t m, const uint32_t *offsets,
   cudaLaunchAttribute attr;
   attr.id = cudaLaunchAttributeCooperative;
   attr.val.cooperative = 1;
-  cudaLaunchConfig_t cfg;
-  std::memset(&cfg, 0, sizeof(cfg));
+  cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(device_sm_count() * std::max(g_static_occ, 1)));
   cfg.blockDim = dim3(kBlock);
   cfg.stream = s;

@@ -754,8 +754,7 @@ int launch_persistent(const void *fn, void **args, int block, int per_sm_req,
     attrs[nattr].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     ++nattr;
   }
-  cudaLaunchConfig_t cfg;
-  std::memset(&cfg, 0, sizeof(cfg));
+  cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(device_sm_count() * per_sm));
   cfg.blockDim = dim3((unsigned)block);
   cfg.stream = s;
