@@ -49,7 +49,7 @@ struct OutTable {
 };
 
 template <int KS>
-__global__ void __launch_bounds__(kBlock) msssp_persistent(Args a) {
+__global__ void __launch_bounds__(kBlock, 8) msssp_persistent(Args a) {
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
   GridSync sync{a.bar, a.v.err, a.timeout_ns};
