@@ -135,6 +135,27 @@ def test_bfs_rmat22_full_size(grus, oracle_mod):
     _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex])
 
 
+@pytest.mark.slow
+def test_bfs_rmat24_full_size_headline(grus, oracle_mod):
+    """The benchmarked configuration: RMAT-24, edge factor 16, seed 3,
+    symmetrised and relabelled, from the first max-degree vertex (the
+    direction-optimising persistent kernel; two pull levels)."""
+    g = grus.Graph.rmat(24, 16, 3, symmetric=True)
+    _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex])
+    g.free()
+
+
+@pytest.mark.slow
+def test_bfs_grid4096_full_size(grus, oracle_mod):
+    """The 4096 x 4096 grid from vertex 4097: 8,189 levels, all but the first
+    64 in the cluster tail."""
+    g = grus.Graph.grid2d(4096, 4096)
+    h = _check_bfs(grus, oracle_mod, g, [4097])
+    d, st = grus.bfs(g, 4097, stats=True)
+    assert st["levels"] == 8189 and st["kernel_launches"] == 2
+    g.free()
+
+
 def _broom(path_len, leaves):
     """A path 0..path_len-1, a star of `leaves` leaves on its last vertex,
     and one further vertex behind every leaf (symmetric CSR)."""

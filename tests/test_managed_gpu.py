@@ -37,3 +37,27 @@ def test_managed_load_gr(grus, tmp_path, oracle_mod):
         assert np.array_equal(grus.sssp(gm, src), oracle_mod.sssp(g, src))
     finally:
         gm.free()
+
+
+@pytest.mark.slow
+def test_managed_rmat26_half_budget_matches_device_mode(grus):
+    """The managed configuration at full size: RMAT-26 (2.1 G edges) with the
+    device budget at half the CSR bytes gives the depths of the same graph
+    held in HBM, with the same reach counts."""
+    torch = pytest.importorskip("torch")
+    g_dev = grus.Graph.rmat(26, 16, 3, symmetric=True)
+    budget = (4 * (g_dev.n + 1) + 4 * g_dev.m) // 2
+    src = g_dev.max_degree_vertex
+    d_dev = torch.empty(g_dev.n, dtype=torch.int32, device="cuda")
+    _, st_dev = grus.bfs(g_dev, src, out=d_dev, stats=True)
+    g_dev.free()
+    g_man = grus.Graph.rmat(26, 16, 3, symmetric=True, managed=True, budget_bytes=budget)
+    assert g_man.max_degree_vertex == src
+    d_man = torch.empty(g_man.n, dtype=torch.int32, device="cuda")
+    _, st_man = grus.bfs(g_man, src, out=d_man, stats=True)
+    assert torch.equal(d_dev, d_man)
+    assert st_man["vertices_reached"] == st_dev["vertices_reached"]
+    assert st_man["edges_reached"] == st_dev["edges_reached"]
+    assert int(d_man[src]) == 0
+    g_man.free()
+
