@@ -57,9 +57,43 @@ __device__ __forceinline__ uint64_t prio(const uint32_t *__restrict__ offs, uint
   return ((uint64_t)(__ldg(offs + x + 1) - __ldg(offs + x)) << 32) | x;
 }
 
+// find_root of two vertices at once: both chains advance in lockstep, so the
+// loads of a step are in flight together (path halving on both).
+__device__ __forceinline__ void find_root2(uint32_t *p, uint32_t &a, uint32_t &b) {
+  uint32_t ya = __ldcg(p + a), yb = __ldcg(p + b);
+  bool da = ya == a, db = yb == b;  // at a root
+  while (!(da && db)) {
+    const uint32_t za = da ? ya : __ldcg(p + ya);
+    const uint32_t zb = db ? yb : __ldcg(p + yb);
+    if (!da) {
+      if (za == ya) {
+        a = ya;
+        da = true;
+      } else {
+        p[a] = za;  // path halving: za is an ancestor of a
+        a = za;
+      }
+    }
+    if (!db) {
+      if (zb == yb) {
+        b = yb;
+        db = true;
+      } else {
+        p[b] = zb;
+        b = zb;
+      }
+    }
+    if (!da) ya = __ldcg(p + a);
+    if (!db) yb = __ldcg(p + b);
+    da = da || ya == a;
+    db = db || yb == b;
+  }
+}
+
 __device__ __forceinline__ void link(const uint32_t *__restrict__ offs, uint32_t *p, uint32_t u,
                                      uint32_t v) {
-  uint32_t ru = find_root(p, u), rv = find_root(p, v);
+  uint32_t ru = u, rv = v;
+  find_root2(p, ru, rv);
   while (ru != rv) {
     if (prio(offs, ru) > prio(offs, rv)) {
       const uint32_t t = ru;
@@ -68,8 +102,8 @@ __device__ __forceinline__ void link(const uint32_t *__restrict__ offs, uint32_t
     }
     const uint32_t old = atomicCAS(p + ru, ru, rv);  // hook lower priority under higher
     if (old == ru) return;
-    ru = find_root(p, old);
-    rv = find_root(p, rv);
+    ru = old;
+    find_root2(p, ru, rv);
   }
 }
 
