@@ -34,7 +34,7 @@
 //     m_f > m_u/alpha, pull->push when n_f < n/beta and the frontier shrinks;
 //     the first push level after a pull level turns the frontier bitmap into
 //     the queue with one atomic per CTA per 256 words.
-//   * narrow tail: a long traversal (64+ levels) whose push frontier and
+//   * narrow tail: a long traversal (16+ levels) whose push frontier and
 //     remaining edges have become small is handed to bfs_narrow, a cluster of
 //     up to 16 CTAs of 1024 threads launched after the persistent kernel,
 //     which runs the remaining levels with one hardware cluster barrier each,
@@ -67,7 +67,7 @@ constexpr float kDefAlpha = 15.f, kDefBeta = 18.f;
 // kNarrowMu edges left whose source is undiscovered, is finished by one
 // thread-block cluster of up to 16 CTAs of 1024 threads.  The edge bound caps
 // the work the cluster may be left with.
-constexpr uint32_t kNarrowAfter = 64;
+constexpr uint32_t kNarrowAfter = 16;
 constexpr uint32_t kNarrowNf = 4096;
 constexpr uint64_t kNarrowMu = 1ull << 26;
 constexpr int kNarrowBlock = 1024;

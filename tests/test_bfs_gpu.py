@@ -148,7 +148,7 @@ def test_bfs_rmat24_full_size_headline(grus, oracle_mod):
 @pytest.mark.slow
 def test_bfs_grid4096_full_size(grus, oracle_mod):
     """The 4096 x 4096 grid from vertex 4097: 8,189 levels, all but the first
-    64 in the cluster tail."""
+    16 in the cluster tail."""
     g = grus.Graph.grid2d(4096, 4096)
     h = _check_bfs(grus, oracle_mod, g, [4097])
     d, st = grus.bfs(g, 4097, stats=True)
