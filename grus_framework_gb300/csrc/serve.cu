@@ -13,8 +13,10 @@
 //     longer than the whole GPU, so a second thread runs the whole-GPU
 //     persistent kernels (grus_bfs / grus_sssp) one launch at a time, and
 //     packs the queued SSSP requests on the same graph -- up to 32 -- into one
-//     multi-source launch (msssp.cu) that writes each request's own output;
-//     BFS requests run as single direction-optimising launches.
+//     multi-source launch (msssp.cu) that writes each request's own output.
+//     BFS requests on one graph are packed -- up to 64, msbfs.cu -- once
+//     enough are queued for the pack to beat single direction-optimising
+//     launches on a graph of that size, else they run alone.
 //     A graph's workspace is allocated only if free HBM covers it plus the
 //     reserve.  Up to four launches are queued on the lane's stream; each
 //     copies its error word to pinned memory and records an event, so the
@@ -230,6 +232,7 @@ size_t big_workspace_bytes(const grus_graph *g, uint32_t algo, bool multi) {
 
 bool big_workspace_ready(const grus_graph *g, uint32_t algo, bool multi) {
   if (algo == GRUS_ALGO_SSSP) return (multi ? g->ws[kWsMsSssp] : g->ws[kWsSssp]) != nullptr;
+  if (multi) return g->ws[kWsMsBfs] != nullptr;
   return multi ? g->ws[kWsMsBfs] != nullptr : g->ws[kWsBfs] != nullptr;
 }
 
@@ -308,6 +311,17 @@ void big_finish(grus_server *s, std::vector<Request> &group, int rc) {
   s->cv.notify_all();
 }
 
+// Fewest queued BFS requests on a graph of m edges for which one multi-source
+// launch beats as many single launches.  Measured on RMAT graphs with random
+// sources: a 16-source pack costs 2.2-5.3 single launches' time up to 2^26
+// edges, 1.1 at 2^27, 0.8 at 2^29, where 32 sources reach 1.3 and 64 2.0.
+uint32_t bfs_pack_min(uint64_t m) {
+  if (m < (1ull << 25)) return 8;
+  if (m < (1ull << 27)) return 16;
+  if (m < (1ull << 28)) return 24;
+  return 32;
+}
+
 void big_scheduler(grus_server *s) {
   cudaSetDevice(s->device);
   constexpr int kDepth = 4;  // launches queued on the lane's stream
@@ -366,10 +380,16 @@ void big_scheduler(grus_server *s) {
         j.group.push_back(first);
         // SSSP requests on one graph share a multi-source launch (it
         // amortises the adjacency reads over up to 32 sources); BFS requests
-        // run alone: one direction-optimising BFS skips most edges, and a
-        // 64-source pack on a small or isolated-source query costs more than
-        // the single launches it replaces
-        const size_t cap = first.algo == GRUS_ALGO_BFS ? 1 : 32;
+        // share one (up to 64) only when enough are queued: a direction-
+        // optimising BFS skips most edges, so a small pack on a big graph
+        // costs more than the single launches it replaces
+        size_t cap = 32;
+        if (first.algo == GRUS_ALGO_BFS) {
+          size_t same = 1;
+          for (const Request &q : s->big_pending)
+            if (q.graph == first.graph && q.algo == GRUS_ALGO_BFS && ++same >= 64) break;
+          cap = same >= bfs_pack_min(s->graphs[first.graph]->m) ? 64 : 1;
+        }
         for (auto it = s->big_pending.begin(); it != s->big_pending.end() && j.group.size() < cap;) {
           if (it->graph == first.graph && it->algo == first.algo) {
             j.group.push_back(*it);
