@@ -19,7 +19,8 @@
 // Queries on graphs of at least big_edges edges do not go to the cluster
 // workers: a 16-CTA worker is a small slice of the GPU and such a query would
 // set the batch's critical path, so they run first as whole-GPU launches
-// (SSSP packed up to 32 sources per multi-source launch).
+// (SSSP packed up to 32 sources per multi-source launch; BFS up to 64 when
+// the graph has enough BFS queries for a pack to beat single launches).
 // Results are bit-exact against single-query runs (BFS depths and SSSP
 // distances are schedule-independent).  The same kernel, launched with one
 // worker on a stream, is the unit of work of the query server (serve.cu).
@@ -558,7 +559,7 @@ struct grus_batch {
   uint32_t member_cap = 0;
   uint32_t group = 1;                  // SSSP queries per multi-source group
   uint32_t ntasks = 0, nmembers = 0;   // of the staged plan
-  uint64_t big_edges = 1ull << 23;     // graphs served by whole-GPU launches
+  uint64_t big_edges = 1ull << 21;     // graphs served by whole-GPU launches
   std::vector<uint8_t> big;            // per graph
   uint32_t *h_errs = nullptr;          // pinned error words of whole-GPU launches
   uint32_t err_cap = 0;
@@ -815,6 +816,7 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(b->ev0, s));
   // queries on big graphs: whole-GPU launches queued first on the stream
   uint32_t nerr = 0;
+  uint32_t nlaunch = 0;  // kernels launched by the big-graph lane
   if (!big_q.empty()) {
     if (b->err_cap < big_q.size()) {
       if (b->h_errs) cudaFreeHost(b->h_errs);
@@ -831,24 +833,34 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
       const grus_query &q0 = queries[big_q[i]];
       grus_graph *g = b->graphs[q0.graph];
       size_t j = i + 1;
-      if (q0.algo == GRUS_ALGO_SSSP)
-        while (j < big_q.size() && j - i < 32 && queries[big_q[j]].graph == q0.graph &&
-               queries[big_q[j]].algo == GRUS_ALGO_SSSP)
-          ++j;
+      const size_t cap = q0.algo == GRUS_ALGO_SSSP ? 32 : 64;
+      while (j < big_q.size() && j - i < cap && queries[big_q[j]].graph == q0.graph &&
+             queries[big_q[j]].algo == q0.algo)
+        ++j;
+      // BFS queries of a graph run alone unless enough share the graph
+      if (q0.algo != GRUS_ALGO_SSSP && j - i < bfs_pack_min(g->m)) j = i + 1;
       CtrlView cv;
       if (j - i == 1) {
         rc = q0.algo == GRUS_ALGO_SSSP ? grus_sssp(g, q0.src, out + q0.out_offset, nullptr, s)
                                        : grus_bfs(g, q0.src, out + q0.out_offset, nullptr, s);
+        // a single BFS is the persistent kernel and its narrow-tail kernel
+        nlaunch += q0.algo == GRUS_ALGO_SSSP ? 1 : 2;
         cv = q0.algo == GRUS_ALGO_SSSP ? sssp_ctrl(g) : bfs_ctrl(g);
       } else {
-        uint32_t srcs[32];
-        uint32_t *outs[32];
+        uint32_t srcs[64];
+        uint32_t *outs[64];
         for (size_t k = i; k < j; ++k) {
           srcs[k - i] = queries[big_q[k]].src;
           outs[k - i] = out + queries[big_q[k]].out_offset;
         }
-        rc = msssp_run(g, srcs, (int)(j - i), outs, nullptr, s);
-        cv = msssp_ctrl(g);
+        ++nlaunch;
+        if (q0.algo == GRUS_ALGO_SSSP) {
+          rc = msssp_run(g, srcs, (int)(j - i), outs, nullptr, s);
+          cv = msssp_ctrl(g);
+        } else {
+          rc = msbfs_run(g, srcs, (int)(j - i), outs, nullptr, s);
+          cv = msbfs_ctrl(g);
+        }
       }
       if (rc) return rc;
       if (cv.ctrl) {
@@ -871,7 +883,7 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
     for (uint32_t i = 0; i < nerr; ++i) bits |= b->h_errs[i];
     if (bits) return status_from_device_error(bits);
     std::memset(stats, 0, sizeof(*stats));
-    stats->kernel_launches = (uint32_t)big_q.size();
+    stats->kernel_launches = nlaunch;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, b->ev0, b->ev1);
     stats->device_ms = ms;
@@ -932,7 +944,7 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
     return status_from_device_error(err);
   }
   std::memset(stats, 0, sizeof(*stats));
-  stats->kernel_launches = 1 + (uint32_t)big_q.size();
+  stats->kernel_launches = 1 + nlaunch;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, b->ev0, b->ev1);
   stats->device_ms = ms;

@@ -87,6 +87,18 @@ int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
 int msssp_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
               grus_stats *stats, cudaStream_t s);
 
+// Fewest BFS queries on one graph of m edges for which one multi-source
+// launch (msbfs_run) beats as many single launches.  Measured on RMAT graphs
+// with random sources: a 16-source pack costs 2.2-5.3 single launches' time
+// up to 2^26 edges, 1.1 at 2^27 and 0.8 at 2^29, where 32 sources reach 1.3
+// and 64 sources 2.0.
+inline uint32_t bfs_pack_min(uint64_t m) {
+  if (m < (1ull << 25)) return 8;
+  if (m < (1ull << 27)) return 16;
+  if (m < (1ull << 28)) return 24;
+  return 32;
+}
+
 // Device control block of a graph's workspace for one algorithm (ctrl null
 // before the algorithm's first call on the graph), for callers that launch
 // without waiting and check the launch's error word later.

@@ -311,17 +311,6 @@ void big_finish(grus_server *s, std::vector<Request> &group, int rc) {
   s->cv.notify_all();
 }
 
-// Fewest queued BFS requests on a graph of m edges for which one multi-source
-// launch beats as many single launches.  Measured on RMAT graphs with random
-// sources: a 16-source pack costs 2.2-5.3 single launches' time up to 2^26
-// edges, 1.1 at 2^27, 0.8 at 2^29, where 32 sources reach 1.3 and 64 2.0.
-uint32_t bfs_pack_min(uint64_t m) {
-  if (m < (1ull << 25)) return 8;
-  if (m < (1ull << 27)) return 16;
-  if (m < (1ull << 28)) return 24;
-  return 32;
-}
-
 void big_scheduler(grus_server *s) {
   cudaSetDevice(s->device);
   constexpr int kDepth = 4;  // launches queued on the lane's stream

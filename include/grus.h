@@ -284,8 +284,9 @@ typedef struct grus_batch_config {
   uint32_t big_edges;    /* queries on graphs with at least this many edges
                             run as whole-GPU launches before the cluster
                             workers start: SSSP packed 32 sources per
-                            launch, BFS one launch each (default 2^23;
-                            0xFFFFFFFF: never) */
+                            launch, BFS up to 64 per launch when enough
+                            share a graph, else one launch each (default
+                            2^21; 0xFFFFFFFF: never) */
 } grus_batch_config;
 
 typedef struct grus_batch grus_batch;

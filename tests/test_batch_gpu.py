@@ -160,3 +160,25 @@ def test_batch_big_graphs_run_whole_gpu(grus, graphs, big_edges):
             ref = reference(grus, graphs, q)
             assert np.array_equal(res[o:o + len(ref)], ref), (big_edges, use_graph, q)
     b.free()
+
+
+def test_batch_packs_bfs_on_whole_gpu_lane(grus, graphs):
+    """With every graph on the whole-GPU lane, 40 BFS queries on one graph run
+    as one 64-source-capable pack and a lone BFS query on another graph as a
+    single launch (persistent kernel + tail): the reported launches are the
+    real ones, and every result equals the single query."""
+    torch = pytest.importorskip("torch")
+    b = grus.Batch(graphs, big_edges=1)
+    rng = np.random.default_rng(17)
+    queries = [(0, grus.ALGO_BFS, int(rng.integers(graphs[0].n))) for _ in range(40)]
+    queries.append((1, grus.ALGO_BFS, 3))
+    offs, total = b.layout(queries)
+    out = torch.full((total,), -5, dtype=torch.int32, device="cuda")
+    st = b.run(queries, out, offs, stats=True)
+    assert st["kernel_launches"] == 1 + 2  # one pack, one single BFS
+    res = out.cpu().numpy().view(np.uint32)
+    for q, o in zip(queries, offs):
+        ref = reference(grus, graphs, q)
+        assert np.array_equal(res[o:o + len(ref)], ref), q
+    b.free()
+
