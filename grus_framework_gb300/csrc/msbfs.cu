@@ -14,8 +14,12 @@
 // then folds the accumulated bits into visit, writes the depths and bins the
 // next frontier.  Pull levels (dense frontiers): each vertex ORs the frontier
 // words of its in-neighbours until every missing source bit is found, with no
-// atomics.  Depths are written as masked stores, one per source bit present
-// in a warp, so 32 consecutive vertices of one source share a store.
+// atomics.  Depths are first kept as one byte per source in a 64-byte row
+// per vertex, written a 16-byte quarter at a time when the vertex gains
+// sources; at the end one pass turns the rows into the per-source outputs,
+// 32 consecutive vertices of one source per store.  (Storing each (vertex,
+// source) depth as it is found leaves partly written sectors at every
+// level.)  Without room for the rows, depths are stored as they are found.
 // Output: depths[k * n + v] (source-major), GRUS_INFINIT where unreached.
 // Bit-exact against k independent BFS runs whatever the schedule.
 #include <algorithm>
@@ -56,6 +60,7 @@ struct Args {
   int k;
   const uint32_t *srcs;
   uint32_t *out[64];  // depth array of each source (n entries each)
+  uint8_t *rows;      // n x 64 depth bytes, or null (direct stores)
   unsigned long long full;
   unsigned long long *visit, *front[2];
   uint32_t *touched[2];
@@ -74,6 +79,54 @@ __device__ __forceinline__ unsigned long long warp_or64(unsigned long long x) {
   const uint32_t lo = __reduce_or_sync(0xffffffffu, (uint32_t)x);
   const uint32_t hi = __reduce_or_sync(0xffffffffu, (uint32_t)(x >> 32));
   return ((unsigned long long)hi << 32) | lo;
+}
+
+// Depth rows: byte s of vertex u's row holds its depth from source s when
+// that depth is 1..kRowMaxDepth; 0 means the depth was stored directly (the
+// source itself, or a vertex first reached deeper).  Bytes of sources that
+// have not reached u are undefined and never read, so rows need no clearing.
+constexpr uint32_t kRowMaxDepth = 254;
+
+// w with the bytes selected by the 4-bit nibble set to fill's bytes
+__device__ __forceinline__ uint32_t byte_merge(uint32_t w, uint32_t nib, uint32_t fill) {
+  const uint32_t m = ((nib * 0x00204081u) & 0x01010101u) * 0xFFu;
+  return (w & ~m) | (fill & m);
+}
+
+// Sets the row bytes of `bits` to `val`; `had` are the sources that reached
+// u before (only quarters holding some of them are read back).
+__device__ __forceinline__ void row_set(const Args &a, uint32_t u, unsigned long long bits,
+                                        unsigned long long had, uint32_t val) {
+  uint4 *row = reinterpret_cast<uint4 *>(a.rows + (size_t)u * 64);
+  const uint32_t fill = val * 0x01010101u;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const uint32_t nb = (uint32_t)(bits >> (16 * q)) & 0xFFFFu;
+    if (!nb) continue;
+    uint4 v = ((had >> (16 * q)) & 0xFFFFull) ? __ldcg(row + q) : make_uint4(0u, 0u, 0u, 0u);
+    v.x = byte_merge(v.x, nb & 0xFu, fill);
+    v.y = byte_merge(v.y, (nb >> 4) & 0xFu, fill);
+    v.z = byte_merge(v.z, (nb >> 8) & 0xFu, fill);
+    v.w = byte_merge(v.w, nb >> 12, fill);
+    row[q] = v;
+  }
+}
+
+// Records depth `val` of u from the sources in `bits` (per lane).
+__device__ __forceinline__ void record_depths(const Args &a, uint32_t u, unsigned long long bits,
+                                              unsigned long long had, uint32_t val) {
+  if (a.rows) {
+    if (val <= kRowMaxDepth) {
+      row_set(a, u, bits, had, val);
+      return;
+    }
+    row_set(a, u, bits, had, 0u);  // stored directly below
+  }
+  while (bits) {
+    const int kb = __ffsll((long long)bits) - 1;
+    bits &= bits - 1;
+    a.out[kb][u] = val;
+  }
 }
 
 // Warp-synchronous: lane's vertex u gets `val` for every source bit in
@@ -131,6 +184,11 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
     bool first = true;
     for (uint32_t j = 0; j < gtid; ++j) first &= a.srcs[j] != s;
     if (first) {
+      if (a.rows) {
+        unsigned long long same = 0;  // every source at s: stored directly above
+        for (int j = 0; j < a.k; ++j) same |= (unsigned long long)(a.srcs[j] == s) << j;
+        row_set(a, s, same, 0ull, 0u);
+      }
       const uint32_t t = atomicAdd(&a.slots[0].tcount, 1u);
       a.touched[0][t] = s;
       const uint32_t b = __ldg(a.offs + s), e = __ldg(a.offs + s + 1);
@@ -168,20 +226,15 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
         if (i < tc) {
           u = __ldcg(tnext + i);
           bits = __ldcg(acc + u);
-          a.visit[u] = __ldcg(a.visit + u) | bits;
+          const unsigned long long had = __ldcg(a.visit + u);
+          a.visit[u] = had | bits;
+          record_depths(a, u, bits, had, val);
           const uint32_t b = __ldg(a.offs + u), e = __ldg(a.offs + u + 1);
           mf += e - b;
           nbits += __popcll(bits);
           if (!push_binned(u, b, e, a.huge, qnext, &nx->qcount, a.cap, cnext, &nx->ccount,
                            a.chunk_cap))
             atomicOr(a.err, kErrOverflow);
-        }
-        // scattered vertices: each lane writes its own bits
-        unsigned long long mine = bits;
-        while (mine) {
-          const int kb = __ffsll((long long)mine) - 1;
-          mine &= mine - 1;
-          a.out[kb][u] = val;
         }
       }
     } else {
@@ -250,7 +303,11 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
               atomicOr(a.err, kErrOverflow);
           }
         }
-        write_depths(a, u, bits, val);
+        if (a.rows) {
+          if (bits) record_depths(a, u, bits, vis, val);
+        } else {
+          write_depths(a, u, bits, val);
+        }
       }
       if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
     }
@@ -288,7 +345,29 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
       nr += c;
       mr += (unsigned long long)c * (__ldg(a.offs + u + 1) - __ldg(a.offs + u));
     }
-    write_depths(a, u, miss, kInfinit);
+    if (!a.rows) {
+      write_depths(a, u, miss, kInfinit);
+      continue;
+    }
+    // the rows become the outputs: per source, 32 consecutive vertices per
+    // store (INFINIT where unreached; a 0 byte was stored directly)
+    const unsigned long long vis = u < a.n ? a.full & ~miss : 0ull;
+    const uint4 *row = reinterpret_cast<const uint4 *>(a.rows + (size_t)u * 64);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (16 * q >= a.k) break;
+      const uint4 v = (u < a.n && ((vis >> (16 * q)) & 0xFFFFull)) ? __ldcg(row + q)
+                                                                    : make_uint4(0u, 0u, 0u, 0u);
+      const uint32_t wd[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int sidx = 16 * q + j;
+        if (sidx >= a.k) break;
+        const bool got = (vis >> sidx) & 1ull;
+        const uint32_t byte = (wd[j >> 2] >> (8 * (j & 3))) & 0xFFu;
+        if (u < a.n && (!got || byte != 0u)) a.out[sidx][u] = got ? byte : kInfinit;
+      }
+    }
   }
   const unsigned long long bnr = block_sum_u64<kBlock>(nr);
   const unsigned long long bmr = block_sum_u64<kBlock>(mr);
@@ -310,6 +389,8 @@ struct Workspace {
   uint32_t *srcs = nullptr;
   uint32_t *depth = nullptr;            // when the caller's buffer is on the host
   size_t depth_bytes = 0;
+  uint8_t *rows = nullptr;              // n x 64 depth bytes
+  bool rows_tried = false;
   char *ctrl = nullptr, *ctrl_host = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
@@ -324,6 +405,7 @@ void ws_free(void *p) {
   cudaFree(w->chunks);
   cudaFree(w->srcs);
   cudaFree(w->depth);
+  cudaFree(w->rows);
   cudaFree(w->ctrl);
   if (w->ctrl_host) cudaFreeHost(w->ctrl_host);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -375,6 +457,14 @@ int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
   Workspace *w = nullptr;
   int rc = ws_get(g, &w);
   if (rc) return rc;
+  if (!w->rows_tried) {
+    // the depth rows; without room for them depths are stored directly
+    w->rows_tried = true;
+    if (cudaMalloc(&w->rows, std::max<uint64_t>(g->n, 1) * 64) != cudaSuccess) {
+      cudaGetLastError();
+      w->rows = nullptr;
+    }
+  }
   static int occ = -1;
   if (occ < 0)
     GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, msbfs_persistent, kBlock, 0));
@@ -391,6 +481,7 @@ int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
   a.k = k;
   a.srcs = w->srcs;
   for (int i = 0; i < k; ++i) a.out[i] = outs[i];
+  a.rows = w->rows;
   a.full = k == 64 ? ~0ull : ((1ull << k) - 1);
   a.visit = w->words;
   a.front[0] = w->words + g->n;

@@ -227,7 +227,8 @@ void scheduler(grus_server *s) {
 size_t big_workspace_bytes(const grus_graph *g, uint32_t algo, bool multi) {
   const size_t n = g->n, m = g->m;
   if (algo == GRUS_ALGO_SSSP && multi) return 128 * n + 16 * n + m / 8 + (1u << 20);
-  return (algo == GRUS_ALGO_SSSP ? 20 * n : 40 * n) + m / 32 + (1u << 20);
+  // a BFS pack also keeps 64 depth bytes per vertex
+  return (algo == GRUS_ALGO_SSSP ? 20 * n : (multi ? 104 * n : 40 * n)) + m / 32 + (1u << 20);
 }
 
 bool big_workspace_ready(const grus_graph *g, uint32_t algo, bool multi) {

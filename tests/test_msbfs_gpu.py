@@ -66,6 +66,17 @@ def test_msbfs_grid(grus, oracle_mod):
     check(grus, oracle_mod, g, srcs)
 
 
+def test_msbfs_depths_beyond_254_levels(grus, oracle_mod):
+    """A 200 x 300 grid (diameter 498) with sources in opposite corners and
+    inside: many vertices are reached by some sources within 254 levels and
+    by others beyond, where depths are stored directly instead of in the
+    per-vertex depth bytes."""
+    g = grus.Graph.grid2d(200, 300)
+    srcs = np.array([0, 200 * 300 - 1, 299, 100 * 300 + 150, 7, 59999, 12345], np.uint32)
+    st = check(grus, oracle_mod, g, srcs)
+    assert st["levels"] > 300
+
+
 def test_msbfs_device_output(grus, oracle_mod):
     torch = pytest.importorskip("torch")
     g = grus.Graph.rmat(11, 16, 8, symmetric=True)
