@@ -18,7 +18,7 @@ namespace grus {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr uint32_t kDefDelta = 640;
+constexpr uint32_t kDefDelta = 1024;
 constexpr int kMaxSources = 32;
 using ms::kPiece;
 using ms::Slot;
