@@ -16,8 +16,8 @@
 // last iteration).  In-degree is binned:
 //   >= kCtaTh (1024) : cut into 2048-edge pieces, one CTA per piece, the
 //                      piece sums added in order afterwards
-//   >= 32            : one warp, loads four wide, shuffle reduction
-//   <  32            : the warp's short lists laid end to end, one edge per
+//   >= kWarpTh (64) : one warp, loads four wide, shuffle reduction
+//   <  kWarpTh      : the warp's short lists laid end to end, one edge per
 //                      lane, segmented warp scan (every lane busy)
 // Per-thread partial sums over more than kKahanTh terms use compensated
 // (Kahan-Babuska) summation; reductions across lanes are pairwise trees.
@@ -36,6 +36,7 @@ constexpr int kBlock = 256;
 constexpr uint32_t kCtaTh = 1024;   // in-degree from which a vertex is "heavy"
 constexpr uint32_t kHChunk = 2048;  // edges per heavy-vertex piece
 constexpr uint32_t kKahanTh = 16;
+constexpr uint32_t kWarpTh = 64;    // in-degree from which a list gets a warp of its own
 constexpr int kShortSteps = 2;      // short-list steps whose gathers are in flight together
 
 struct Args {
@@ -118,7 +119,7 @@ __device__ __forceinline__ float gather_seq(const Args &a, const float *cs, uint
   return comp ? k.value() : s;
 }
 
-// The short lists (< 32 in-edges) of a warp's vertices, laid end to end:
+// The short lists (< kWarpTh in-edges) of a warp's vertices, laid end to end:
 // lane k of a step takes edge k of the concatenation (coalesced source-id
 // loads, every lane busy), a segmented warp scan sums each vertex's run
 // within the step (a fixed pairwise order), and the owning lane adds its
@@ -242,7 +243,7 @@ __global__ void __launch_bounds__(kBlock, 8) pr_persistent(Args a) {
       }
       bool done = v >= a.n || end - beg >= kCtaTh;
       while (true) {
-        const uint32_t ball = __ballot_sync(0xffffffffu, !done && end - beg >= 32);
+        const uint32_t ball = __ballot_sync(0xffffffffu, !done && end - beg >= kWarpTh);
         if (!ball) break;
         const int leader = __ffs(ball) - 1;
         const uint32_t wv = __shfl_sync(0xffffffffu, v, leader);
