@@ -27,6 +27,7 @@ namespace grus {
 
 constexpr uint32_t kChunk = 1024;  // edges per chunk work item
 constexpr uint32_t kCtaTh = 256;   // CTA-cooperative degree threshold
+constexpr uint32_t kWarpTh = 32;   // warp-cooperative degree threshold
 
 // Appends vertex v (adjacency [b,e)) to the binned lists of a frontier.
 // Degree-0 vertices are not enqueued (nothing to expand).  Returns false on
@@ -137,7 +138,7 @@ __device__ __forceinline__ void expand_tile(uint32_t v, uint32_t beg, uint32_t e
   }
   // warp-cooperative
   while (true) {
-    const uint32_t ball = __ballot_sync(0xffffffffu, end - beg >= 32);
+    const uint32_t ball = __ballot_sync(0xffffffffu, end - beg >= kWarpTh);
     if (!ball) break;
     const int leader = __ffs(ball) - 1;
     const uint32_t ws = __shfl_sync(0xffffffffu, v, leader);
