@@ -113,7 +113,7 @@ class Tuning(C.Structure):
     _fields_ = [
         ("alpha", C.c_float), ("beta", C.c_float), ("ctas_per_sm", C.c_uint32),
         ("huge_degree", C.c_uint32), ("bu_scan", C.c_uint32), ("timeout_ms", C.c_uint32),
-        ("sssp_delta", C.c_uint32), ("bu_words", C.c_uint32),
+        ("sssp_delta", C.c_uint32), ("bu_words", C.c_uint32), ("multi_alpha", C.c_float),
     ]
 
 
@@ -394,7 +394,10 @@ class Graph:
     def set_tuning(self, **kw):
         t = Tuning()
         _check(lib.grus_graph_get_tuning(self._handle(), C.byref(t)), "grus_graph_get_tuning")
+        known = {f for f, _ in t._fields_}
         for k, v in kw.items():
+            if k not in known:
+                raise TypeError(f"unknown tuning field {k!r}")
             setattr(t, k, v)
         _check(lib.grus_graph_set_tuning(self._handle(), C.byref(t)), "grus_graph_set_tuning")
 

@@ -34,7 +34,14 @@ namespace {
 constexpr int kBlock = 256;
 constexpr uint32_t kPullLane = 32;  // in-edges a lane scans alone in a pull level
 constexpr uint32_t kDefHuge = 1024;
-constexpr float kDefAlpha = 15.f;
+// Pull once the frontier's out-edges exceed m / alpha.  A pull level scans
+// in-lists until every missing source bit is found, so it costs more the more
+// sources a launch carries and the switch comes later for wide launches.
+// Measured on RMAT-20/22/23/24: with 64 sources alpha 2-10 is flat and 15
+// pulls one level too early (RMAT-23: 12.7 -> 6.0 ms); with 8-16 sources
+// alpha 5 is 5 % slower than 10-15 on RMAT-20; 7-10 suits every width.
+constexpr float kDefAlpha = 10.f;      // up to 32 sources
+constexpr float kDefAlphaWide = 6.f;   // 33-64 sources
 
 struct Slot {
   uint32_t tcount;        // touched / frontier list length of the level
@@ -499,7 +506,7 @@ int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
   a.bar = (GridBarrier *)(w->ctrl + kOffBar);
   a.err = (uint32_t *)(w->ctrl + kOffErr);
   a.summary = (Summary *)(w->ctrl + kOffSummary);
-  a.alpha = tune_or(g->tuning.alpha, kDefAlpha);
+  a.alpha = tune_or(g->tuning.multi_alpha, k > 32 ? kDefAlphaWide : kDefAlpha);
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
   GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffSummary, 0, kCtrlBytes - kOffSummary, s));
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));

@@ -109,6 +109,9 @@ typedef struct grus_tuning {
   uint32_t timeout_ms;    /* bound on every device-side wait */
   uint32_t sssp_delta;    /* SSSP near/far bucket width (distance units) */
   uint32_t bu_words;      /* BFS pull levels: bitmap words per warp step (2 or 4) */
+  float multi_alpha;      /* multi-source BFS: push->pull when the union frontier's
+                             out-edges exceed m / multi_alpha (0: 10 up to 32
+                             sources, 6 above) */
 } grus_tuning;
 
 /* ---- library ------------------------------------------------------------- */
@@ -349,8 +352,9 @@ GRUS_API int grus_telemetry_sample(grus_telemetry *out);
  * hbm_reserve_bytes; admitted queries overlap on the device.  Big graphs: a
  * second thread queues whole-GPU persistent launches back to back on a
  * high-priority stream, and packs the queued SSSP queries on the same graph
- * (up to 32) into one multi-source launch; a graph's workspace is allocated only if free HBM covers it plus
- * the reserve.  Latency is measured from submit to observed completion on the
+ * (up to 32) into one multi-source launch, and the queued BFS queries on it
+ * (up to 64) when enough are queued; a graph's workspace is allocated only
+ * if free HBM covers it plus the reserve.  Latency is measured from submit to observed completion on the
  * host clock. */
 typedef struct grus_server grus_server;
 

@@ -65,3 +65,34 @@ def test_package_import_fails_loudly_without_library(tmp_path, monkeypatch):
         mod.version()
     with pytest.raises(ImportError):
         mod.Graph.rmat(8)
+
+
+STRUCTS = {"Stats": "grus_stats", "GraphInfo": "grus_graph_info", "LevelTrace": "grus_level_trace",
+           "Query": "grus_query", "BatchConfig": "grus_batch_config", "ServerConfig": "grus_server_config",
+           "Completion": "grus_completion", "ServerStats": "grus_server_stats",
+           "Telemetry": "grus_telemetry", "Tuning": "grus_tuning"}
+
+
+def test_ctypes_structs_match_header(tmp_path):
+    """Every ctypes mirror in the package has the C struct's size and each of
+    its fields the C field's offset and size, as gcc lays out include/grus.h."""
+    import subprocess
+    import grus_framework_gb300 as pkg
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "grus.h"', "int main(void) {"]
+    expect = []
+    for py, c in STRUCTS.items():
+        cls = getattr(pkg, py)
+        lines.append(f'  printf("%zu\\n", sizeof({c}));')
+        expect.append(ctypes.sizeof(cls))
+        for name, _ in cls._fields_:
+            f = getattr(cls, name)
+            lines.append(f'  printf("%zu %zu\\n", offsetof({c}, {name}), sizeof((({c} *)0)->{name}));')
+            expect.append(f"{f.offset} {f.size}")
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")[:-1]
+    assert got == [str(e) for e in expect]
+

@@ -46,7 +46,7 @@ def test_msbfs_repeated_and_isolated_sources(grus, oracle_mod):
 @pytest.mark.parametrize("alpha", [1e9, 1e-3])
 def test_msbfs_push_only_and_pull_heavy(grus, oracle_mod, alpha):
     g = grus.Graph.rmat(13, 16, 9, symmetric=True)
-    g.set_tuning(alpha=alpha)
+    g.set_tuning(multi_alpha=alpha)
     srcs = np.arange(0, 64 * 97, 97, dtype=np.uint32) % g.n
     check(grus, oracle_mod, g, srcs)
 
@@ -56,7 +56,7 @@ def test_msbfs_directed_with_and_without_csc(grus, oracle_mod):
     srcs = np.arange(64, dtype=np.uint32) * 61 % g.n
     check(grus, oracle_mod, g, srcs)
     g.build_csc()
-    g.set_tuning(alpha=1e-3)
+    g.set_tuning(multi_alpha=1e-3)
     check(grus, oracle_mod, g, srcs)
 
 
