@@ -670,6 +670,7 @@ def run_batch(args, dist, rank, local):
                "queries": nq, "sources": "degree > 0, seed 4", "sum_n": int(sum(g.n for g in gs)),
                "sum_m": int(sum(g.m for g in gs)), "workers": info["workers"],
                "cluster_size": info["cluster_size"], "big_edges": info["big_edges"],
+               "launch_entries": info["launch_entries"],
                "l2": "flushed (256 MB write) before each step", "parallelism": f"replicas x{dist.get_world_size() if dist else 1}"}
         result = {
             "metric": w["metric"], "value": round(value, 1), "unit": QPS,

@@ -79,7 +79,8 @@ class Query(C.Structure):
 class BatchConfig(C.Structure):
     _fields_ = [("cluster_size", C.c_uint32), ("workers", C.c_uint32),
                 ("huge_degree", C.c_uint32), ("sssp_delta", C.c_uint32),
-                ("group_sources", C.c_uint32), ("big_edges", C.c_uint32)]
+                ("group_sources", C.c_uint32), ("big_edges", C.c_uint32),
+                ("launch_entries", C.c_uint32)]
 
 
 class ServerConfig(C.Structure):
@@ -529,9 +530,10 @@ class Batch:
     (cluster workers, include/grus.h grus_batch_*)."""
 
     def __init__(self, graphs, cluster_size=0, workers=0, huge_degree=0, sssp_delta=0,
-                 group_sources=0, big_edges=0):
+                 group_sources=0, big_edges=0, launch_entries=0):
         self.graphs = list(graphs)
-        cfg = BatchConfig(cluster_size, workers, huge_degree, sssp_delta, group_sources, big_edges)
+        cfg = BatchConfig(cluster_size, workers, huge_degree, sssp_delta, group_sources, big_edges,
+                          launch_entries)
         h = C.c_void_p()
         _check(lib.grus_batch_create(_graph_array(self.graphs), len(self.graphs), C.byref(cfg),
                                      C.byref(h)), "grus_batch_create")

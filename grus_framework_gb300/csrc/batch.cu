@@ -18,9 +18,12 @@
 //          such groups.
 // Queries on graphs of at least big_edges edges do not go to the cluster
 // workers: a 16-CTA worker is a small slice of the GPU and such a query would
-// set the batch's critical path, so they run first as whole-GPU launches
-// (SSSP packed up to 32 sources per multi-source launch; BFS up to 64 when
-// the graph has enough BFS queries for a pack to beat single launches).
+// set the batch's critical path, so they run first as whole-GPU launches.
+// SSSP: up to 32 queries per graph form a pack, and the packs of up to 64
+// graphs share ONE multi-graph multi-source launch (msssp.cu), so the graphs'
+// levels overlap instead of following one another; BFS: up to 64 sources per
+// launch when the graph has enough BFS queries for a pack to beat single
+// launches, else one launch each.
 // Results are bit-exact against single-query runs (BFS depths and SSSP
 // distances are schedule-independent).  The same kernel, launched with one
 // worker on a stream, is the unit of work of the query server (serve.cu).
@@ -560,9 +563,11 @@ struct grus_batch {
   uint32_t group = 1;                  // SSSP queries per multi-source group
   uint32_t ntasks = 0, nmembers = 0;   // of the staged plan
   uint64_t big_edges = 1ull << 21;     // graphs served by whole-GPU launches
+  uint64_t launch_entries = 1ull << 23;  // distance entries per multi-graph launch
   std::vector<uint8_t> big;            // per graph
   uint32_t *h_errs = nullptr;          // pinned error words of whole-GPU launches
   uint32_t err_cap = 0;
+  void *uws = nullptr;                 // multi-graph SSSP launches' workspace
   grus::BatchState state;
   int cluster = 16, workers = 0;
   uint32_t huge = 1024, delta = 192;
@@ -578,6 +583,131 @@ struct grus_batch {
 };
 
 using namespace grus;
+
+// SSSP queries on big graphs (big_q sorted by graph): packs of up to 32 per
+// graph; round r takes every graph's r-th pack and runs as multi-graph
+// launches of at most kMaxUnion graphs whose distance rows total at most
+// launch_entries (a launch left with one graph runs as that graph's own
+// multi-source launch, or as a single query).  The cap keeps a launch's
+// distance rows in L2: the 32 graphs of a C4b batch in one launch (368 MB of
+// rows) took 48.7 ms against 37 ms as one launch per graph.  Each launch's
+// error word is copied to h_errs.
+static int union_sssp(grus_batch *b, const grus_query *queries, const std::vector<int> &big_q,
+                      uint32_t *out, cudaStream_t s, uint32_t *nerr, uint32_t *nlaunch) {
+  struct Pack {
+    uint32_t graph;
+    std::vector<int> q;
+  };
+  std::vector<std::vector<Pack>> rounds;
+  for (size_t i = 0; i < big_q.size();) {
+    const uint32_t gi = queries[big_q[i]].graph;
+    size_t j = i;
+    std::vector<int> qs;
+    while (j < big_q.size() && queries[big_q[j]].graph == gi) {
+      if (queries[big_q[j]].algo == GRUS_ALGO_SSSP) qs.push_back(big_q[j]);
+      ++j;
+    }
+    for (size_t r = 0; r * 32 < qs.size(); ++r) {
+      if (rounds.size() <= r) rounds.emplace_back();
+      Pack p;
+      p.graph = gi;
+      p.q.assign(qs.begin() + r * 32, qs.begin() + std::min(qs.size(), (r + 1) * 32));
+      rounds[r].push_back(std::move(p));
+    }
+    i = j;
+  }
+  if (rounds.empty()) return GRUS_OK;
+  // split rounds into launches
+  const uint64_t kMaxEntries = b->launch_entries;
+  std::vector<std::vector<const Pack *>> launches;
+  uint64_t max_v = 0, max_m = 0;
+  uint32_t max_ks = 8;
+  for (const auto &rd : rounds) {
+    std::vector<const Pack *> cur;
+    uint64_t v = 0, m = 0;
+    uint32_t kmax = 0;
+    auto flush = [&]() {
+      if (cur.empty()) return;
+      if (cur.size() > 1) {
+        max_v = std::max(max_v, v);
+        max_m = std::max(max_m, m);
+        const uint32_t ks = kmax <= 8 ? 8u : (kmax <= 16 ? 16u : 32u);
+        max_ks = std::max(max_ks, ks);
+      }
+      launches.push_back(cur);
+      cur.clear();
+      v = m = 0;
+      kmax = 0;
+    };
+    for (const Pack &p : rd) {
+      const grus_graph *g = b->graphs[p.graph];
+      const uint32_t k2 = std::max<uint32_t>(kmax, (uint32_t)p.q.size());
+      const uint32_t ks2 = k2 <= 8 ? 8u : (k2 <= 16 ? 16u : 32u);
+      if (!cur.empty() && (cur.size() >= (size_t)ms::kMaxUnion || (v + g->n) * ks2 > kMaxEntries ||
+                           v + g->n >= 0xFFFFFFF0ull || v + m / ms::kPiece + g->n + g->m / ms::kPiece +
+                           1024 >= 0xFFFFFFF0ull))
+        flush();
+      cur.push_back(&p);
+      v += g->n;
+      m += g->m;
+      kmax = std::max<uint32_t>(kmax, (uint32_t)p.q.size());
+    }
+    flush();
+  }
+  int nunion = 0;
+  for (const auto &l : launches) nunion += l.size() > 1;
+  if (nunion) {
+    int rc = msssp_union_reserve(&b->uws, nunion, max_v, max_m, max_ks);
+    if (rc) return rc;
+  }
+  int region = 0;
+  for (const auto &l : launches) {
+    CtrlView cv;
+    int rc;
+    if (l.size() == 1) {
+      const Pack &p = *l[0];
+      grus_graph *g = b->graphs[p.graph];
+      if (p.q.size() == 1) {
+        const grus_query &q = queries[p.q[0]];
+        rc = grus_sssp(g, q.src, out + q.out_offset, nullptr, s);
+        cv = sssp_ctrl(g);
+      } else {
+        uint32_t srcs[32];
+        uint32_t *outs[32];
+        for (size_t k = 0; k < p.q.size(); ++k) {
+          srcs[k] = queries[p.q[k]].src;
+          outs[k] = out + queries[p.q[k]].out_offset;
+        }
+        rc = msssp_run(g, srcs, (int)p.q.size(), outs, nullptr, s);
+        cv = msssp_ctrl(g);
+      }
+    } else {
+      grus_graph *gs[ms::kMaxUnion];
+      uint32_t kq[ms::kMaxUnion];
+      std::vector<uint32_t> srcs;
+      std::vector<uint32_t *> outs;
+      for (size_t i = 0; i < l.size(); ++i) {
+        gs[i] = b->graphs[l[i]->graph];
+        kq[i] = (uint32_t)l[i]->q.size();
+        for (int qi : l[i]->q) {
+          srcs.push_back(queries[qi].src);
+          outs.push_back(out + queries[qi].out_offset);
+        }
+      }
+      rc = msssp_union_run(b->uws, region++, gs, (int)l.size(), kq, srcs.data(), outs.data(), 0, s,
+                           &cv);
+    }
+    if (rc) return rc;
+    ++*nlaunch;
+    if (cv.ctrl) {
+      GRUS_CUDA_TRY(cudaMemcpyAsync(b->h_errs + *nerr, cv.ctrl + cv.err_off, 4,
+                                    cudaMemcpyDeviceToHost, s));
+      GRUS_CUDA_TRY(cudaMemsetAsync(cv.ctrl + cv.err_off, 0, 4, s));
+      ++*nerr;
+    }
+  }
+  return GRUS_OK;
+}
 
 extern "C" {
 
@@ -606,6 +736,7 @@ int grus_batch_create(grus_graph *const *graphs, int ngraphs, const grus_batch_c
     if (cfg->sssp_delta) b->delta = cfg->sssp_delta;
     if (cfg->workers) b->workers = (int)cfg->workers;
     if (cfg->group_sources) b->group = cfg->group_sources;
+    if (cfg->launch_entries) b->launch_entries = cfg->launch_entries;
   }
   if (b->group < 1 || b->group > (uint32_t)kMaxGroup) {
     delete b;
@@ -776,6 +907,7 @@ static int stage_tasks(grus_batch *b, const grus_query *q, int nq) {
   return GRUS_OK;
 }
 
+
 int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *out,
                    int use_graph, grus_stats *stats, void *stream) {
   if (!b || !queries || nq < 0 || !out) return GRUS_EINVAL;
@@ -829,8 +961,14 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
       if (queries[x].graph != queries[y].graph) return queries[x].graph < queries[y].graph;
       return queries[x].algo < queries[y].algo;
     });
+    rc = union_sssp(b, queries, big_q, out, s, &nerr, &nlaunch);
+    if (rc) return rc;
     for (size_t i = 0; i < big_q.size();) {
       const grus_query &q0 = queries[big_q[i]];
+      if (q0.algo == GRUS_ALGO_SSSP) {  // launched by union_sssp
+        ++i;
+        continue;
+      }
       grus_graph *g = b->graphs[q0.graph];
       size_t j = i + 1;
       const size_t cap = q0.algo == GRUS_ALGO_SSSP ? 32 : 64;
@@ -881,7 +1019,10 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
     GRUS_CUDA_TRY(cudaStreamSynchronize(s));
     uint32_t bits = 0;
     for (uint32_t i = 0; i < nerr; ++i) bits |= b->h_errs[i];
-    if (bits) return status_from_device_error(bits);
+    if (bits) {
+      msssp_union_reset(b->uws);
+      return status_from_device_error(bits);
+    }
     std::memset(stats, 0, sizeof(*stats));
     stats->kernel_launches = nlaunch;
     float ms = 0.f;
@@ -941,6 +1082,7 @@ int grus_batch_run(grus_batch *b, const grus_query *queries, int nq, uint32_t *o
   for (uint32_t i = 0; i < nerr; ++i) err |= b->h_errs[i];
   if (err) {
     cudaMemset(b->state.err, 0, 4);
+    msssp_union_reset(b->uws);
     return status_from_device_error(err);
   }
   std::memset(stats, 0, sizeof(*stats));
@@ -960,6 +1102,7 @@ int grus_batch_get_info(const grus_batch *b, grus_batch_config *info) {
   info->sssp_delta = b->delta;
   info->group_sources = b->group;
   info->big_edges = b->big_edges >= 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)b->big_edges;
+  info->launch_entries = (uint32_t)b->launch_entries;
   return GRUS_OK;
 }
 
@@ -969,6 +1112,7 @@ int grus_batch_free(grus_batch *b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   b->state.release();
+  grus::msssp_union_free(b->uws);
   cudaFree(b->d_graphs);
   cudaFree(b->d_tasks);
   if (b->h_tasks) cudaFreeHost(b->h_tasks);

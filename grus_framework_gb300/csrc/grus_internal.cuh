@@ -111,4 +111,19 @@ CtrlView sssp_ctrl(grus_graph *g);
 CtrlView msbfs_ctrl(grus_graph *g);
 CtrlView msssp_ctrl(grus_graph *g);
 
+// Multi-graph multi-source SSSP (msssp.cu): ONE whole-GPU launch over ng
+// (<= 64) weighted graphs, graph g with kq[g] (1..32) sources; srcs and outs
+// list the sources and their n_g-entry device outputs graph after graph.
+// The workspace belongs to the caller: reserve it for `regions` launches of
+// at most max_v vertices, max_m edges and ks (8/16/32) sources per graph
+// before the first launch of a run; launch i of a run uses region i.  *cv
+// receives the launch's control block (error word).
+int msssp_union_reserve(void **ws, int regions, uint64_t max_v, uint64_t max_m, uint32_t ks);
+int msssp_union_run(void *ws, int region, grus_graph *const *gs, int ng, const uint32_t *kq,
+                    const uint32_t *srcs, uint32_t *const *outs, uint32_t delta, cudaStream_t s,
+                    CtrlView *cv);
+void msssp_union_free(void *ws);
+// Clears the control blocks after a failed launch.
+void msssp_union_reset(void *ws);
+
 }  // namespace grus

@@ -69,6 +69,44 @@ __global__ void __launch_bounds__(kBlock, 8) msssp_persistent(Args a) {
   }
 }
 
+// Multi-graph launch: the same level loop over several graphs at once
+// (msssp_core.cuh, kUnion); the vertex bases go to shared memory for the
+// graph lookups.
+struct UnionArgs {
+  ms::View v;
+  GridBarrier *bar;
+  Summary *summary;
+  uint64_t timeout_ns;
+};
+
+struct NoOut {
+  __device__ __forceinline__ uint32_t *operator()(uint32_t) const { return nullptr; }
+};
+
+template <int KS>
+__global__ void __launch_bounds__(kBlock, 8) msssp_union(UnionArgs a) {
+  __shared__ uint32_t s_vb[ms::kMaxUnion + 1];
+  for (uint32_t i = threadIdx.x; i <= a.v.ngraphs; i += kBlock)
+    s_vb[i] = i < a.v.ngraphs ? a.v.ug[i].vbase : a.v.n;
+  __syncthreads();
+  const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
+  const uint32_t nthreads = gridDim.x * kBlock;
+  GridSync sync{a.bar, a.v.err, a.timeout_ns};
+  ms::Result r;
+  if (!ms::run<KS, kBlock, true>(a.v, gtid, nthreads, sync, NoOut{}, r, s_vb)) return;
+  const unsigned long long bnr = block_sum_u64<kBlock>(r.nr);
+  const unsigned long long bmr = block_sum_u64<kBlock>(r.mr);
+  if (threadIdx.x == 0) {
+    atomicAdd(&a.summary->nr, bnr);
+    atomicAdd(&a.summary->mr, bmr);
+  }
+  if (gtid == 0) {
+    a.summary->levels = r.levels;
+    a.summary->splits = r.splits;
+    a.summary->visits = r.visits;
+  }
+}
+
 struct Workspace {
   uint32_t ks = 0;             // row width the distance matrix was sized for
   uint32_t *D = nullptr;       // n * ks
@@ -219,6 +257,172 @@ int msssp_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
   float ms = 0.f;
   cudaEventElapsedTime(&ms, w->ev0, w->ev1);
   stats->device_ms = ms;
+  return GRUS_OK;
+}
+
+// ---- multi-graph launches --------------------------------------------------
+// The caller (a batch) owns the workspace: distance matrix and masks sized for
+// the largest launch, and per-launch regions for the graph table and the
+// sources, so that several launches queued in one run never share staging.
+struct UnionWs {
+  uint64_t d_entries = 0;      // capacity of D in u32
+  uint64_t vcap = 0;           // vertices the masks cover
+  uint32_t *D = nullptr, *masks = nullptr;
+  uint4 *ent = nullptr;
+  uint64_t ent_cap = 0;
+  int regions = 0;             // launches one run may queue
+  ms::UnionGraph *ug = nullptr, *ug_host = nullptr;        // regions * kMaxUnion
+  uint32_t *seeds = nullptr, *seeds_host = nullptr;        // regions * 2 * kSeedCap
+  char *ctrl = nullptr;        // regions * kCtrlBytes
+};
+
+constexpr uint32_t kSeedCap = ms::kMaxUnion * kMaxSources;
+
+void msssp_union_free(void *p) {
+  UnionWs *w = (UnionWs *)p;
+  if (!w) return;
+  cudaFree(w->D);
+  cudaFree(w->masks);
+  cudaFree(w->ent);
+  cudaFree(w->ug);
+  cudaFree(w->seeds);
+  cudaFree(w->ctrl);
+  if (w->ug_host) cudaFreeHost(w->ug_host);
+  if (w->seeds_host) cudaFreeHost(w->seeds_host);
+  delete w;
+}
+
+// After a launch reported an error its barrier words may be left mid-count:
+// clear every region's control block (the stream has been synchronised).
+void msssp_union_reset(void *p) {
+  UnionWs *w = (UnionWs *)p;
+  if (w && w->ctrl) cudaMemset(w->ctrl, 0, (size_t)w->regions * kCtrlBytes);
+}
+
+int msssp_union_reserve(void **wsp, int regions, uint64_t max_v, uint64_t max_m, uint32_t ks) {
+  UnionWs *w = (UnionWs *)*wsp;
+  const uint64_t v1 = std::max<uint64_t>(max_v, 1);
+  const uint64_t ecap = v1 + max_m / kPiece + 1024;
+  if (ecap > 0xFFFFFFF0ull || v1 >= 0xFFFFFFFFull) {
+    set_last_error("multi-graph sssp launch too large");
+    return GRUS_EINVAL;
+  }
+  if (w && w->regions >= regions && w->vcap >= v1 && w->d_entries >= v1 * ks && w->ent_cap >= ecap)
+    return GRUS_OK;
+  if (w) cudaDeviceSynchronize();  // launches of an earlier run may still use it
+  UnionWs *nw = new UnionWs();
+  nw->regions = std::max(regions, w ? w->regions : 0);
+  nw->vcap = std::max(v1, w ? w->vcap : 0);
+  nw->d_entries = std::max(v1 * ks, w ? w->d_entries : 0);
+  nw->ent_cap = std::max(ecap, w ? w->ent_cap : 0);
+  msssp_union_free(w);
+  *wsp = nullptr;
+  cudaError_t e = cudaMalloc(&nw->D, nw->d_entries * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&nw->masks, 3 * nw->vcap * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&nw->ent, nw->ent_cap * sizeof(uint4));
+  if (e == cudaSuccess) e = cudaMalloc(&nw->ug, (size_t)nw->regions * ms::kMaxUnion * sizeof(ms::UnionGraph));
+  if (e == cudaSuccess) e = cudaMalloc(&nw->seeds, (size_t)nw->regions * 2 * kSeedCap * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&nw->ctrl, (size_t)nw->regions * kCtrlBytes);
+  if (e == cudaSuccess) e = cudaMemset(nw->ctrl, 0, (size_t)nw->regions * kCtrlBytes);
+  if (e == cudaSuccess)
+    e = cudaMallocHost(&nw->ug_host, (size_t)nw->regions * ms::kMaxUnion * sizeof(ms::UnionGraph));
+  if (e == cudaSuccess) e = cudaMallocHost(&nw->seeds_host, (size_t)nw->regions * 2 * kSeedCap * 4);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    msssp_union_free(nw);
+    set_last_error(std::string("multi-graph sssp workspace: ") + cudaGetErrorString(e));
+    return status_from_cuda(e);
+  }
+  *wsp = nw;
+  return GRUS_OK;
+}
+
+template <int KS>
+int launch_union(UnionWs *w, UnionArgs &a, uint64_t nv, cudaStream_t s) {
+  static int occ = -1;
+  if (occ < 0)
+    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, msssp_union<KS>, kBlock, 0));
+  void *args[] = {&a};
+  return launch_persistent((const void *)msssp_union<KS>, args, kBlock, 0, occ, s, w->masks,
+                           (size_t)3 * nv * 4);
+}
+
+int msssp_union_run(void *wsp, int region, grus_graph *const *gs, int ng, const uint32_t *kq,
+                    const uint32_t *srcs, uint32_t *const *outs, uint32_t delta, cudaStream_t s,
+                    CtrlView *cv) {
+  UnionWs *w = (UnionWs *)wsp;
+  if (!w || region < 0 || region >= w->regions || ng < 1 || ng > ms::kMaxUnion) return GRUS_EINVAL;
+  ms::UnionGraph *ugh = w->ug_host + (size_t)region * ms::kMaxUnion;
+  uint32_t *sv = w->seeds_host + (size_t)region * 2 * kSeedCap, *ss = sv + kSeedCap;
+  uint64_t V = 0, M = 0;
+  uint32_t kmax = 0, nseeds = 0;
+  for (int g = 0; g < ng; ++g) {
+    const grus_graph *G = gs[g];
+    if (!G || !G->csr.wts || kq[g] < 1 || kq[g] > (uint32_t)kMaxSources) return GRUS_EINVAL;
+    std::memset(&ugh[g], 0, sizeof(ugh[g]));
+    ugh[g].offs = G->csr.offs;
+    ugh[g].cols = G->csr.cols;
+    ugh[g].wts = G->csr.wts;
+    ugh[g].vbase = (uint32_t)V;
+    ugh[g].k = kq[g];
+    for (uint32_t i = 0; i < kq[g]; ++i) {
+      const uint32_t src = srcs[nseeds];
+      if (src >= G->n || !outs[nseeds]) return GRUS_EINVAL;
+      ugh[g].out[i] = outs[nseeds];
+      sv[nseeds] = (uint32_t)V + src;
+      ss[nseeds] = i;
+      ++nseeds;
+    }
+    V += G->n;
+    M += G->m;
+    kmax = std::max(kmax, kq[g]);
+  }
+  const uint32_t ks = kmax <= 8 ? 8u : (kmax <= 16 ? 16u : 32u);
+  if (V == 0 || V > w->vcap || V * ks > w->d_entries || V + M / kPiece + 1024 > w->ent_cap) {
+    set_last_error("multi-graph sssp workspace too small for the launch");
+    return GRUS_EINVAL;
+  }
+  ms::UnionGraph *ugd = w->ug + (size_t)region * ms::kMaxUnion;
+  uint32_t *sd = w->seeds + (size_t)region * 2 * kSeedCap;
+  char *ctrl = w->ctrl + (size_t)region * kCtrlBytes;
+  GRUS_CUDA_TRY(cudaMemcpyAsync(ugd, ugh, ng * sizeof(ms::UnionGraph), cudaMemcpyHostToDevice, s));
+  GRUS_CUDA_TRY(cudaMemcpyAsync(sd, sv, nseeds * 4, cudaMemcpyHostToDevice, s));
+  GRUS_CUDA_TRY(cudaMemcpyAsync(sd + kSeedCap, ss, nseeds * 4, cudaMemcpyHostToDevice, s));
+  GRUS_CUDA_TRY(cudaMemsetAsync(ctrl + kOffSummary, 0, kCtrlBytes - kOffSummary, s));
+  UnionArgs a;
+  std::memset((void *)&a, 0, sizeof(a));
+  a.v.n = (uint32_t)V;
+  a.v.k = kmax;
+  a.v.srcs = sd;
+  a.v.seed_slot = sd + kSeedCap;
+  a.v.nseeds = nseeds;
+  a.v.ug = ugd;
+  a.v.ngraphs = (uint32_t)ng;
+  a.v.D = w->D;
+  a.v.F[0] = w->masks;
+  a.v.F[1] = w->masks + V;
+  a.v.far = w->masks + 2 * V;
+  a.v.ent = w->ent;
+  a.v.ent_cap = (uint32_t)std::min<uint64_t>(w->ent_cap, 0xFFFFFFF0ull);
+  a.v.slots = (Slot *)(ctrl + kOffSlots);
+  a.v.minfar = (uint32_t *)(ctrl + kOffFar);
+  a.v.err = (uint32_t *)(ctrl + kOffErr);
+  a.v.delta = std::max(1u, delta ? delta : kDefDelta);
+  a.bar = (GridBarrier *)(ctrl + kOffBar);
+  a.summary = (Summary *)(ctrl + kOffSummary);
+  a.timeout_ns = 30000ull * 1000000ull;
+  int rc;
+  switch (ks) {
+    case 8: rc = launch_union<8>(w, a, V, s); break;
+    case 16: rc = launch_union<16>(w, a, V, s); break;
+    default: rc = launch_union<32>(w, a, V, s); break;
+  }
+  if (rc) return rc;
+  if (cv) {
+    cv->ctrl = ctrl;
+    cv->bytes = kCtrlBytes;
+    cv->err_off = kOffErr;
+  }
   return GRUS_OK;
 }
 

@@ -24,6 +24,16 @@
 // already expanded and are dropped, pairs below the new T move to F.
 // Each (v, s) pair reaches Dijkstra's distance whatever the schedule, so the
 // outputs are bit-exact against single-source runs.
+//
+// Multi-graph launches (kUnion): several graphs share one launch and one
+// level loop.  Their vertices are numbered one after another (graph g owns
+// ids vb[g] .. vb[g+1]-1), D, F and Far cover all of them, and each graph
+// brings its own sources in slots 0..k_g-1.  A vertex's graph is found by a
+// binary search over the bases in shared memory; work entries keep the
+// graph's own edge indices and a relaxation adds the graph's base to the
+// column id.  No edge joins two graphs, so every graph's distances are the
+// same as in a launch of its own; the threshold T is shared, which only
+// changes the schedule.
 #pragma once
 
 #include "device_util.cuh"
@@ -43,6 +53,16 @@ struct Slot {                         // 32 bytes
   uint32_t pad[2];
 };
 
+constexpr int kMaxUnion = 64;         // graphs per multi-graph launch
+
+// One graph of a multi-graph launch.
+struct UnionGraph {
+  const uint32_t *offs, *cols, *wts;
+  uint32_t vbase;                     // first id of the graph's vertices
+  uint32_t k;                         // its sources (slots 0..k-1)
+  uint32_t *out[32];                  // output of slot s: n_g distances
+};
+
 struct View {
   const uint32_t *__restrict__ offs;
   const uint32_t *__restrict__ cols;
@@ -58,7 +78,24 @@ struct View {
   uint32_t *minfar;                   // 2, by split parity
   uint32_t *err;
   uint32_t delta;
+  // multi-graph launches only: graphs, and the slot of each of the nseeds
+  // sources in srcs (global ids)
+  const UnionGraph *ug = nullptr;
+  uint32_t ngraphs = 0, nseeds = 0;
+  const uint32_t *seed_slot = nullptr;
 };
+
+// Graph of vertex v: the largest g with vb[g] <= v (vb[ng] is the vertex
+// count, above every id).
+__device__ __forceinline__ uint32_t graph_of(const uint32_t *vb, uint32_t ng, uint32_t v) {
+  uint32_t lo = 0, hi = ng;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (vb[mid] <= v) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
 
 struct Result {
   uint32_t levels = 0, splits = 0;
@@ -66,9 +103,9 @@ struct Result {
 };
 
 // Step 1: vertices with a non-empty near mask become work entries.
-template <int kBlock>
-__device__ __forceinline__ void build_entries(const View &a, uint32_t *F, Slot *sl, uint32_t tid,
-                                              uint32_t nthreads) {
+template <int kBlock, bool kUnion>
+__device__ __forceinline__ void build_entries(const View &a, const uint32_t *vb, uint32_t *F,
+                                              Slot *sl, uint32_t tid, uint32_t nthreads) {
   const uint32_t rounds = (a.n + nthreads - 1) / nthreads;
   __shared__ uint32_t s_base;
   for (uint32_t r = 0; r < rounds; ++r) {
@@ -78,8 +115,15 @@ __device__ __forceinline__ void build_entries(const View &a, uint32_t *F, Slot *
       m = __ldcg(F + v);
       if (m) {
         F[v] = 0u;
-        b = __ldg(a.offs + v);
-        e = __ldg(a.offs + v + 1);
+        const uint32_t *offs = a.offs;
+        uint32_t lv = v;
+        if constexpr (kUnion) {
+          const uint32_t g = graph_of(vb, a.ngraphs, v);
+          offs = a.ug[g].offs;
+          lv = v - vb[g];
+        }
+        b = __ldg(offs + lv);
+        e = __ldg(offs + lv + 1);
         nch = (e - b + kPiece - 1) / kPiece;
       }
     }
@@ -104,11 +148,19 @@ __device__ __forceinline__ void build_entries(const View &a, uint32_t *F, Slot *
 // entry's mask do work: the lanes are dealt (edge, active source) pairs,
 // lane = j * p + i takes the i-th active source of edge j, so a warp step
 // covers floor(32 / p) edges and every lane of it relaxes a live pair.
-template <int KS>
-__device__ __forceinline__ unsigned long long relax_entry(const View &a, const uint4 ent,
-                                                          uint32_t *Fn, uint32_t T) {
+template <int KS, bool kUnion>
+__device__ __forceinline__ unsigned long long relax_entry(const View &a, const uint32_t *vb,
+                                                          const uint4 ent, uint32_t *Fn, uint32_t T) {
   const uint32_t lane = lane_id();
   const uint32_t u = ent.x, b = ent.y, e = ent.z, mask = ent.w;
+  const uint32_t *cols = a.cols, *wts = a.wts;
+  uint32_t vbase = 0;
+  if constexpr (kUnion) {
+    const uint32_t g = graph_of(vb, a.ngraphs, u);
+    cols = a.ug[g].cols;
+    wts = a.ug[g].wts;
+    vbase = vb[g];
+  }
   const uint32_t p = __popc(mask);
   // distance of u from source `lane`, handed to the lanes by shuffle
   const uint32_t du_all = (lane < (uint32_t)KS && ((mask >> lane) & 1u))
@@ -121,8 +173,8 @@ __device__ __forceinline__ unsigned long long relax_entry(const View &a, const u
   const uint32_t bit = 1u << (s & 31u);
   for (uint32_t x0 = b; x0 < e; x0 += 32) {
     const uint32_t xi = x0 + lane;
-    const uint32_t c = xi < e ? __ldg(a.cols + xi) : 0u;
-    const uint32_t w = xi < e ? __ldg(a.wts + xi) : 0u;
+    const uint32_t c = xi < e ? __ldg(cols + xi) + vbase : 0u;
+    const uint32_t w = xi < e ? __ldg(wts + xi) : 0u;
     const uint32_t ne = min(32u, e - x0);
     for (uint32_t j0 = 0; j0 < ne; j0 += 4 * eps) {
       uint32_t v[4], nd[4], cur[4];
@@ -153,10 +205,12 @@ __device__ __forceinline__ unsigned long long relax_entry(const View &a, const u
 
 // The whole traversal over the threads [0, nthreads) of one group (a grid or
 // a cluster); `sync` is the group barrier (returns false when it gave up) and
-// `out(s)` the output array of source s.  Returns false if a barrier failed.
-template <int KS, int kBlock, class Sync, class Out>
+// `out(s)` the output array of source s (one graph; a multi-graph launch
+// writes through a.ug and takes the vertex bases vb, shared memory, ngraphs+1
+// entries).  Returns false if a barrier failed.
+template <int KS, int kBlock, bool kUnion = false, class Sync, class Out>
 __device__ __forceinline__ bool run(const View &a, uint32_t tid, uint32_t nthreads, Sync &sync,
-                                    const Out &out, Result &res) {
+                                    const Out &out, Result &res, const uint32_t *vb = nullptr) {
   const uint32_t gwarp = tid >> 5, nwarps = nthreads >> 5;
   // prologue
   const size_t dn = (size_t)a.n * KS;
@@ -169,7 +223,13 @@ __device__ __forceinline__ bool run(const View &a, uint32_t tid, uint32_t nthrea
   if (tid < 4 * sizeof(Slot) / 4) ((uint32_t *)a.slots)[tid] = 0u;
   if (tid < 2) a.minfar[tid] = 0xFFFFFFFFu;
   if (!sync()) return false;
-  if (tid < a.k) {
+  if constexpr (kUnion) {
+    for (uint32_t i = tid; i < a.nseeds; i += nthreads) {
+      const uint32_t src = a.srcs[i], slot = a.seed_slot[i];
+      a.D[(size_t)src * KS + slot] = 0u;
+      atomicOr(a.F[0] + src, 1u << slot);
+    }
+  } else if (tid < a.k) {
     const uint32_t src = a.srcs[tid];
     a.D[(size_t)src * KS + tid] = 0u;
     atomicOr(a.F[0] + src, 1u << tid);
@@ -182,7 +242,7 @@ __device__ __forceinline__ bool run(const View &a, uint32_t tid, uint32_t nthrea
     Slot *sl = a.slots + (L & 3u);
     // reset the slot used two levels ahead
     if (tid < sizeof(Slot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[tid] = 0u;
-    build_entries<kBlock>(a, a.F[sel], sl, tid, nthreads);
+    build_entries<kBlock, kUnion>(a, vb, a.F[sel], sl, tid, nthreads);
     if (!sync()) return false;
     const uint32_t nent = min(__ldcg(&sl->nent), a.ent_cap);
     if (nent == 0) {
@@ -243,7 +303,8 @@ __device__ __forceinline__ bool run(const View &a, uint32_t tid, uint32_t nthrea
     }
     uint32_t *Fn = a.F[sel ^ 1u];
     unsigned long long lv = 0;
-    for (uint32_t i = gwarp; i < nent; i += nwarps) lv += relax_entry<KS>(a, __ldcg(a.ent + i), Fn, T);
+    for (uint32_t i = gwarp; i < nent; i += nwarps)
+      lv += relax_entry<KS, kUnion>(a, vb, __ldcg(a.ent + i), Fn, T);
     const unsigned long long bv = block_sum_u64<kBlock>(lv);
     if (threadIdx.x == 0 && bv) atomicAdd(&sl->visits, bv);
     if (!sync()) return false;
@@ -257,14 +318,31 @@ __device__ __forceinline__ bool run(const View &a, uint32_t tid, uint32_t nthrea
   }
   // epilogue: outputs (source-major) and this thread's reach counts
   unsigned long long nr = 0, mr = 0;
-  for (uint32_t v = tid; v < a.n; v += nthreads) {
-    const uint32_t deg = __ldg(a.offs + v + 1) - __ldg(a.offs + v);
-    for (uint32_t s = 0; s < a.k; ++s) {
-      const uint32_t d = __ldcg(a.D + (size_t)v * KS + s);
-      out(s)[v] = d;
-      if (d != kInf) {
-        ++nr;
-        mr += deg;
+  if constexpr (kUnion) {
+    for (uint32_t v = tid; v < a.n; v += nthreads) {
+      const uint32_t g = graph_of(vb, a.ngraphs, v);
+      const UnionGraph &G = a.ug[g];
+      const uint32_t lv = v - vb[g];
+      const uint32_t deg = __ldg(G.offs + lv + 1) - __ldg(G.offs + lv);
+      for (uint32_t s = 0; s < G.k; ++s) {
+        const uint32_t d = __ldcg(a.D + (size_t)v * KS + s);
+        G.out[s][lv] = d;
+        if (d != kInf) {
+          ++nr;
+          mr += deg;
+        }
+      }
+    }
+  } else {
+    for (uint32_t v = tid; v < a.n; v += nthreads) {
+      const uint32_t deg = __ldg(a.offs + v + 1) - __ldg(a.offs + v);
+      for (uint32_t s = 0; s < a.k; ++s) {
+        const uint32_t d = __ldcg(a.D + (size_t)v * KS + s);
+        out(s)[v] = d;
+        if (d != kInf) {
+          ++nr;
+          mr += deg;
+        }
       }
     }
   }

@@ -286,10 +286,15 @@ typedef struct grus_batch_config {
                             graphs) */
   uint32_t big_edges;    /* queries on graphs with at least this many edges
                             run as whole-GPU launches before the cluster
-                            workers start: SSSP packed 32 sources per
-                            launch, BFS up to 64 per launch when enough
+                            workers start: SSSP packed up to 32 sources
+                            per graph, BFS up to 64 per launch when enough
                             share a graph, else one launch each (default
                             2^21; 0xFFFFFFFF: never) */
+  uint32_t launch_entries;/* the SSSP packs of several of those graphs share
+                            one launch while their distance rows (vertices
+                            x 8/16/32 sources) total at most this many
+                            entries (default 2^23 = 32 MiB, which stays in
+                            L2; 1: one graph per launch) */
 } grus_batch_config;
 
 typedef struct grus_batch grus_batch;

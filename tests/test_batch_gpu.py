@@ -182,3 +182,57 @@ def test_batch_packs_bfs_on_whole_gpu_lane(grus, graphs):
         assert np.array_equal(res[o:o + len(ref)], ref), q
     b.free()
 
+
+
+def test_batch_sssp_packs_share_one_launch_across_graphs(grus, graphs):
+    """With every graph on the whole-GPU lane, the SSSP packs of several
+    graphs (32 + 8 queries on one graph, 1, 8, 3 with a repeated source, and
+    17 on the grid) run as ONE multi-graph launch for the first packs and the
+    second pack of the 40-query graph on its own; a BFS query is a single
+    launch (persistent kernel + tail).  Every result equals the single query."""
+    torch = pytest.importorskip("torch")
+    b = grus.Batch(graphs, big_edges=1)
+    rng = np.random.default_rng(23)
+    S, B = grus.ALGO_SSSP, grus.ALGO_BFS
+    queries = [(0, S, int(rng.integers(graphs[0].n))) for _ in range(40)]
+    queries += [(1, S, 5)]
+    queries += [(2, S, int(rng.integers(graphs[2].n))) for _ in range(8)]
+    queries += [(5, S, 9), (5, S, 9), (5, S, 0)]
+    queries += [(6, S, int(rng.integers(graphs[6].n))) for _ in range(17)]
+    queries += [(3, B, 4)]
+    order = rng.permutation(len(queries))
+    queries = [queries[i] for i in order]
+    offs, total = b.layout(queries)
+    out = torch.full((total,), -3, dtype=torch.int32, device="cuda")
+    st = b.run(queries, out, offs, stats=True)
+    assert st["kernel_launches"] == 2 + 2
+    res = out.cpu().numpy().view(np.uint32)
+    for q, o in zip(queries, offs):
+        ref = reference(grus, graphs, q)
+        assert np.array_equal(res[o:o + len(ref)], ref), q
+    # the same batch again reuses the launch workspace
+    out2 = torch.full((total,), -4, dtype=torch.int32, device="cuda")
+    b.run(queries, out2, offs, stats=True)
+    assert torch.equal(out, out2)
+    b.free()
+
+
+def test_batch_multi_graph_launches_split_past_64_graphs(grus):
+    """66 small graphs with one SSSP query each on the whole-GPU lane: a launch
+    takes at most 64 graphs, so the queries run as two multi-graph launches,
+    and every result equals the single query."""
+    torch = pytest.importorskip("torch")
+    gs = [grus.Graph.rmat(6 + i % 3, 4, 500 + i, symmetric=True, weighted=True) for i in range(66)]
+    b = grus.Batch(gs, big_edges=1)
+    queries = [(i, grus.ALGO_SSSP, (7 * i) % gs[i].n) for i in range(66)]
+    offs, total = b.layout(queries)
+    out = torch.full((total,), -1, dtype=torch.int32, device="cuda")
+    st = b.run(queries, out, offs, stats=True)
+    assert st["kernel_launches"] == 2
+    res = out.cpu().numpy().view(np.uint32)
+    for (gi, _, src), o in zip(queries, offs):
+        ref = grus.sssp(gs[gi], src)
+        assert np.array_equal(res[o:o + len(ref)], ref), gi
+    b.free()
+    for g in gs:
+        g.free()
