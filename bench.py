@@ -24,9 +24,9 @@ events.
 Other workloads (`--workload`): sssp-rmat22, cc-rmat22, pagerank-rmat24
 (directed), bfs-grid4096, bfs-rmat26-managed (managed memory, device budget
 half the CSR bytes), msbfs-rmat23 (64 sources), msssp-rmat22 (32 sources),
-and the two systems forms in queries/s: batch-c4b (256 SSSP queries over 32
+and the two systems forms in queries/s: batch-sssp256 (256 SSSP queries over 32
 resident RMAT graphs of scales 14-20 in one batched call per step; also the
-same queries as back-to-back plain calls) and serve-c5 (Poisson arrivals at
+same queries as back-to-back plain calls) and serve-mixed (Poisson arrivals at
 8,000 queries/s against 8 resident RMAT graphs of scales 16-24, half SSSP,
 through the query server; a step is 1,000 queries; p50/p99 latency, a sweep
 of lower arrival rates, and back-to-back plain calls of the same mix).
@@ -59,8 +59,8 @@ FALLBACK_HBM_GBS = 6800.0
 UNIT = "GTEPS"
 INFINIT = 4294967294
 
-# Graph sets of the batched (C4b) and served (C5) workloads: (scale, edge
-# factor, generator seed), symmetrised, weighted, relabelled.
+# Graph sets of the batched and served workloads: (scale, edge factor,
+# generator seed), symmetrised, weighted, relabelled.
 def batch_graph_specs(seed):
     rng = np.random.default_rng(seed)
     specs = []
@@ -111,11 +111,11 @@ WORKLOADS = {
                                managed=True, budget_fraction=0.5,
                                metric="GTEPS (single-query BFS, RMAT-26 symmetrised, managed "
                                       "memory, device budget 50% of the CSR bytes)"),
-    "batch-c4b": dict(algo="batch", graph="rmat-set", seed=4, queries=256, kernel="batch_kernel "
+    "batch-sssp256": dict(algo="batch", graph="rmat-set", seed=4, queries=256, kernel="batch_kernel "
                       "(cluster workers) + msssp_persistent (graphs of 2^21+ edges)",
                       metric="queries/s (256 SSSP queries over 32 resident RMAT graphs, scales "
                              "14-20, edge factors 8-32, one batched call)"),
-    "serve-c5": dict(algo="serve", graph="rmat-set", seed=5, rate=8000, sweep_rates=[500, 2000],
+    "serve-mixed": dict(algo="serve", graph="rmat-set", seed=5, rate=8000, sweep_rates=[500, 2000],
                      sweep_queries=2000, step_queries=1000, sssp_fraction=0.5,
                      kernel="server lanes: batch_kernel slots + whole-GPU bfs/sssp/msssp launches",
                      metric="queries/s served (Poisson arrivals at 8,000/s, 8 resident RMAT graphs "
@@ -538,7 +538,7 @@ def run_grus(args, dist, rank, local):
 
 
 # ---------------------------------------------------------------------------
-# batched (C4b) and served (C5) forms
+# batched and served forms
 QPS = "queries/s"
 
 

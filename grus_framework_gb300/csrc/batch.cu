@@ -589,8 +589,8 @@ using namespace grus;
 // launches of at most kMaxUnion graphs whose distance rows total at most
 // launch_entries (a launch left with one graph runs as that graph's own
 // multi-source launch, or as a single query).  The cap keeps a launch's
-// distance rows in L2: the 32 graphs of a C4b batch in one launch (368 MB of
-// rows) took 48.7 ms against 37 ms as one launch per graph.  Each launch's
+// distance rows in L2: 256 queries over 32 RMAT graphs of scales 14-20 in one
+// launch (368 MB of rows) took 48.7 ms against 37 ms as one launch per graph.  Each launch's
 // error word is copied to h_errs.
 static int union_sssp(grus_batch *b, const grus_query *queries, const std::vector<int> &big_q,
                       uint32_t *out, cudaStream_t s, uint32_t *nerr, uint32_t *nlaunch) {

@@ -63,8 +63,8 @@ def test_batch_cuda_graph_replay(grus, graphs):
 
 
 def test_batch_256_sssp_over_32_graphs(grus):
-    """The C4b shape at small scale: 256 SSSP queries over 32 resident graphs
-    of mixed scale and edge factor."""
+    """256 SSSP queries over 32 resident graphs of mixed scale and edge
+    factor, at small scale."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(4)
     gs = [grus.Graph.rmat(int(rng.integers(8, 13)), int(rng.choice([8, 16, 32])), 500 + i,

@@ -1,8 +1,8 @@
 """GPU: device generator and BFS against the CPU oracle, through the C ABI.
 
 BFS depths are integer results and must match bit for bit (the fixpoint of
-samples/bfs/bfs.cu:18-87), on the golden fixtures, on RMAT-16 (the C1
-configuration), on directed and high-diameter graphs, and -- through the
+samples/bfs/bfs.cu:18-87), on the golden fixtures, on RMAT-16 (edge factor
+16, seed 1, symmetrised), on directed and high-diameter graphs, and -- through the
 size-independent checks that the serial oracle can afford -- on RMAT-22.
 """
 import json
@@ -72,7 +72,7 @@ def _check_bfs(grus, oracle_mod, g, srcs):
 
 
 def test_bfs_rmat16_c1(grus, oracle_mod):
-    """C1: RMAT scale 16, ef 16, seed 1, symmetrised, source = max-degree vertex."""
+    """RMAT scale 16, ef 16, seed 1, symmetrised, source = max-degree vertex."""
     g = grus.Graph.rmat(16, 16, 1, symmetric=True)
     rng = np.random.default_rng(0)
     _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, *rng.integers(0, g.n, 4)])

@@ -62,6 +62,6 @@ def test_pagerank_hub_heavy_graph(grus, oracle_mod):
 
 @pytest.mark.slow
 def test_pagerank_rmat24_c3a(grus, oracle_mod):
-    """C3a: directed RMAT-24 ef16 seed 3, d=0.85, 20 iterations."""
+    """Directed RMAT-24 ef16 seed 3, d=0.85, 20 iterations."""
     g = grus.Graph.rmat(24, 16, 3, symmetric=False)
     check(grus, oracle_mod, g)

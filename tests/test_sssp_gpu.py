@@ -2,8 +2,8 @@
 
 Distances over integer weights are the unique fixpoint of the relax of
 samples/sssp/sssp.cu:51-60 and must match bit for bit, for every bucket width
-(Delta), launch shape and graph family, and on the C2 configuration
-(RMAT-22, weights in [1,255]).
+(Delta), launch shape and graph family, and on RMAT-22 (edge factor 16,
+seed 2, weights in [1,255]).
 """
 import json
 
@@ -71,6 +71,6 @@ def test_sssp_unweighted_graph_rejected(grus):
 
 @pytest.mark.slow
 def test_sssp_rmat22_c2(grus, oracle_mod):
-    """C2: RMAT-22 ef16 seed 2 symmetrised, weights in [1,255]."""
+    """RMAT-22 ef16 seed 2 symmetrised, weights in [1,255]."""
     g = grus.Graph.rmat(22, 16, 2, symmetric=True, weighted=True)
     check(grus, oracle_mod, g, [g.max_degree_vertex])
