@@ -71,7 +71,7 @@ def _check_bfs(grus, oracle_mod, g, srcs):
     return h
 
 
-def test_bfs_rmat16_c1(grus, oracle_mod):
+def test_bfs_rmat16(grus, oracle_mod):
     """RMAT scale 16, ef 16, seed 1, symmetrised, source = max-degree vertex."""
     g = grus.Graph.rmat(16, 16, 1, symmetric=True)
     rng = np.random.default_rng(0)

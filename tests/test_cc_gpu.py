@@ -53,7 +53,7 @@ def test_cc_repeatable(grus, oracle_mod):
 
 
 @pytest.mark.slow
-def test_cc_rmat22_c2(grus, oracle_mod):
+def test_cc_rmat22_full_size(grus, oracle_mod):
     """RMAT-22 ef16 seed 2 symmetrised."""
     g = grus.Graph.rmat(22, 16, 2, symmetric=True, weighted=True)
     assert np.array_equal(grus.cc(g), oracle_mod.cc(host_csr(g)))

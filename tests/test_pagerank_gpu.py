@@ -61,7 +61,7 @@ def test_pagerank_hub_heavy_graph(grus, oracle_mod):
 
 
 @pytest.mark.slow
-def test_pagerank_rmat24_c3a(grus, oracle_mod):
+def test_pagerank_rmat24_full_size(grus, oracle_mod):
     """Directed RMAT-24 ef16 seed 3, d=0.85, 20 iterations."""
     g = grus.Graph.rmat(24, 16, 3, symmetric=False)
     check(grus, oracle_mod, g)

@@ -70,7 +70,7 @@ def test_sssp_unweighted_graph_rejected(grus):
 
 
 @pytest.mark.slow
-def test_sssp_rmat22_c2(grus, oracle_mod):
+def test_sssp_rmat22_full_size(grus, oracle_mod):
     """RMAT-22 ef16 seed 2 symmetrised, weights in [1,255]."""
     g = grus.Graph.rmat(22, 16, 2, symmetric=True, weighted=True)
     check(grus, oracle_mod, g, [g.max_degree_vertex])
