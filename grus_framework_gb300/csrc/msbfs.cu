@@ -14,9 +14,9 @@
 // then folds the accumulated bits into visit, writes the depths and bins the
 // next frontier.  Pull levels (dense frontiers): each vertex ORs the frontier
 // words of its in-neighbours until every missing source bit is found, with no
-// atomics.  Depths are first kept as one byte per source in a 64-byte row
-// per vertex, written a 16-byte quarter at a time when the vertex gains
-// sources; at the end one pass turns the rows into the per-source outputs,
+// atomics.  Depths are first kept as one byte per source in a row per
+// vertex (16 bytes per 16 sources of the launch), written a 16-byte quarter
+// at a time when the vertex gains sources; at the end one pass turns the rows into the per-source outputs,
 // 32 consecutive vertices of one source per store.  (Storing each (vertex,
 // source) depth as it is found leaves partly written sectors at every
 // level.)  Without room for the rows, depths are stored as they are found.
@@ -67,7 +67,8 @@ struct Args {
   int k;
   const uint32_t *srcs;
   uint32_t *out[64];  // depth array of each source (n entries each)
-  uint8_t *rows;      // n x 64 depth bytes, or null (direct stores)
+  uint8_t *rows;      // n rows of row_bytes depth bytes, or null (direct stores)
+  uint32_t row_bytes; // 16 per 16 sources: 16, 32, 48 or 64
   unsigned long long full;
   unsigned long long *visit, *front[2];
   uint32_t *touched[2];
@@ -104,7 +105,7 @@ __device__ __forceinline__ uint32_t byte_merge(uint32_t w, uint32_t nib, uint32_
 // u before (only quarters holding some of them are read back).
 __device__ __forceinline__ void row_set(const Args &a, uint32_t u, unsigned long long bits,
                                         unsigned long long had, uint32_t val) {
-  uint4 *row = reinterpret_cast<uint4 *>(a.rows + (size_t)u * 64);
+  uint4 *row = reinterpret_cast<uint4 *>(a.rows + (size_t)u * a.row_bytes);
   const uint32_t fill = val * 0x01010101u;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -359,7 +360,7 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
     // the rows become the outputs: per source, 32 consecutive vertices per
     // store (INFINIT where unreached; a 0 byte was stored directly)
     const unsigned long long vis = u < a.n ? a.full & ~miss : 0ull;
-    const uint4 *row = reinterpret_cast<const uint4 *>(a.rows + (size_t)u * 64);
+    const uint4 *row = reinterpret_cast<const uint4 *>(a.rows + (size_t)u * a.row_bytes);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       if (16 * q >= a.k) break;
@@ -489,6 +490,8 @@ int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
   a.srcs = w->srcs;
   for (int i = 0; i < k; ++i) a.out[i] = outs[i];
   a.rows = w->rows;
+  // rows as wide as the sources need, so narrow launches share sectors
+  a.row_bytes = 16u * (((uint32_t)k + 15u) / 16u);
   a.full = k == 64 ? ~0ull : ((1ull << k) - 1);
   a.visit = w->words;
   a.front[0] = w->words + g->n;
