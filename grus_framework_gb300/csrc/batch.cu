@@ -590,8 +590,8 @@ using namespace grus;
 // launch_entries (a launch left with one graph runs as that graph's own
 // multi-source launch, or as a single query).  The cap keeps a launch's
 // distance rows in L2: 256 queries over 32 RMAT graphs of scales 14-20 in one
-// launch (368 MB of rows) took 48.7 ms against 37 ms as one launch per graph.  Each launch's
-// error word is copied to h_errs.
+// launch (368 MB of rows) took 48.7 ms against 37 ms as one launch per graph.
+// Each launch's error word is copied to h_errs.
 static int union_sssp(grus_batch *b, const grus_query *queries, const std::vector<int> &big_q,
                       uint32_t *out, cudaStream_t s, uint32_t *nerr, uint32_t *nlaunch) {
   struct Pack {
@@ -618,7 +618,7 @@ static int union_sssp(grus_batch *b, const grus_query *queries, const std::vecto
   }
   if (rounds.empty()) return GRUS_OK;
   // split rounds into launches
-  const uint64_t kMaxEntries = b->launch_entries;
+  const uint64_t cap = b->launch_entries;  // distance entries per launch
   std::vector<std::vector<const Pack *>> launches;
   uint64_t max_v = 0, max_m = 0;
   uint32_t max_ks = 8;
@@ -643,7 +643,7 @@ static int union_sssp(grus_batch *b, const grus_query *queries, const std::vecto
       const grus_graph *g = b->graphs[p.graph];
       const uint32_t k2 = std::max<uint32_t>(kmax, (uint32_t)p.q.size());
       const uint32_t ks2 = k2 <= 8 ? 8u : (k2 <= 16 ? 16u : 32u);
-      if (!cur.empty() && (cur.size() >= (size_t)ms::kMaxUnion || (v + g->n) * ks2 > kMaxEntries ||
+      if (!cur.empty() && (cur.size() >= (size_t)ms::kMaxUnion || (v + g->n) * ks2 > cap ||
                            v + g->n >= 0xFFFFFFF0ull || v + m / ms::kPiece + g->n + g->m / ms::kPiece +
                            1024 >= 0xFFFFFFF0ull))
         flush();
