@@ -39,6 +39,7 @@
 #include "expand.cuh"
 #include "grus_internal.cuh"
 #include "msssp_core.cuh"
+#include "union_plan.h"
 
 namespace cg = cooperative_groups;
 
@@ -584,88 +585,39 @@ struct grus_batch {
 
 using namespace grus;
 
-// SSSP queries on big graphs (big_q sorted by graph): packs of up to 32 per
-// graph; round r takes every graph's r-th pack and runs as multi-graph
-// launches of at most kMaxUnion graphs whose distance rows total at most
-// launch_entries (a launch left with one graph runs as that graph's own
-// multi-source launch, or as a single query).  The cap keeps a launch's
-// distance rows in L2: 256 queries over 32 RMAT graphs of scales 14-20 in one
-// launch (368 MB of rows) took 48.7 ms against 37 ms as one launch per graph.
-// Each launch's error word is copied to h_errs.
+// SSSP queries on big graphs (big_q sorted by graph), grouped into launches
+// by plan_union (union_plan.h): up to 32 per graph per pack, several graphs'
+// packs per multi-graph launch while their distance rows total at most
+// launch_entries.  The cap keeps a launch's distance rows in L2: 256 queries
+// over 32 RMAT graphs of scales 14-20 in one launch (368 MB of rows) took
+// 48.7 ms against 37 ms as one launch per graph.  Each launch's error word is
+// copied to h_errs.
 static int union_sssp(grus_batch *b, const grus_query *queries, const std::vector<int> &big_q,
                       uint32_t *out, cudaStream_t s, uint32_t *nerr, uint32_t *nlaunch) {
-  struct Pack {
-    uint32_t graph;
-    std::vector<int> q;
-  };
-  std::vector<std::vector<Pack>> rounds;
-  for (size_t i = 0; i < big_q.size();) {
-    const uint32_t gi = queries[big_q[i]].graph;
-    size_t j = i;
-    std::vector<int> qs;
-    while (j < big_q.size() && queries[big_q[j]].graph == gi) {
-      if (queries[big_q[j]].algo == GRUS_ALGO_SSSP) qs.push_back(big_q[j]);
-      ++j;
-    }
-    for (size_t r = 0; r * 32 < qs.size(); ++r) {
-      if (rounds.size() <= r) rounds.emplace_back();
-      Pack p;
-      p.graph = gi;
-      p.q.assign(qs.begin() + r * 32, qs.begin() + std::min(qs.size(), (r + 1) * 32));
-      rounds[r].push_back(std::move(p));
-    }
-    i = j;
+  std::vector<int> sssp;
+  for (int qi : big_q)
+    if (queries[qi].algo == GRUS_ALGO_SSSP) sssp.push_back(qi);
+  if (sssp.empty()) return GRUS_OK;
+  std::vector<uint32_t> qgraph(*std::max_element(sssp.begin(), sssp.end()) + 1);
+  for (int qi : sssp) qgraph[qi] = queries[qi].graph;
+  std::vector<uint64_t> gn(b->graphs.size()), gm(b->graphs.size());
+  for (size_t g = 0; g < b->graphs.size(); ++g) {
+    gn[g] = b->graphs[g]->n;
+    gm[g] = b->graphs[g]->m;
   }
-  if (rounds.empty()) return GRUS_OK;
-  // split rounds into launches
-  const uint64_t cap = b->launch_entries;  // distance entries per launch
-  std::vector<std::vector<const Pack *>> launches;
-  uint64_t max_v = 0, max_m = 0;
-  uint32_t max_ks = 8;
-  for (const auto &rd : rounds) {
-    std::vector<const Pack *> cur;
-    uint64_t v = 0, m = 0;
-    uint32_t kmax = 0;
-    auto flush = [&]() {
-      if (cur.empty()) return;
-      if (cur.size() > 1) {
-        max_v = std::max(max_v, v);
-        max_m = std::max(max_m, m);
-        const uint32_t ks = kmax <= 8 ? 8u : (kmax <= 16 ? 16u : 32u);
-        max_ks = std::max(max_ks, ks);
-      }
-      launches.push_back(cur);
-      cur.clear();
-      v = m = 0;
-      kmax = 0;
-    };
-    for (const Pack &p : rd) {
-      const grus_graph *g = b->graphs[p.graph];
-      const uint32_t k2 = std::max<uint32_t>(kmax, (uint32_t)p.q.size());
-      const uint32_t ks2 = k2 <= 8 ? 8u : (k2 <= 16 ? 16u : 32u);
-      if (!cur.empty() && (cur.size() >= (size_t)ms::kMaxUnion || (v + g->n) * ks2 > cap ||
-                           v + g->n >= 0xFFFFFFF0ull || v + m / ms::kPiece + g->n + g->m / ms::kPiece +
-                           1024 >= 0xFFFFFFF0ull))
-        flush();
-      cur.push_back(&p);
-      v += g->n;
-      m += g->m;
-      kmax = std::max<uint32_t>(kmax, (uint32_t)p.q.size());
-    }
-    flush();
-  }
-  int nunion = 0;
-  for (const auto &l : launches) nunion += l.size() > 1;
-  if (nunion) {
-    int rc = msssp_union_reserve(&b->uws, nunion, max_v, max_m, max_ks);
+  const UnionPlan plan =
+      plan_union(sssp, qgraph, gn, gm, b->launch_entries, (size_t)ms::kMaxUnion, ms::kPiece);
+  if (plan.unions) {
+    int rc = msssp_union_reserve(&b->uws, plan.unions, plan.max_v, plan.max_m, plan.max_ks);
     if (rc) return rc;
   }
+  const auto &launches = plan.launches;
   int region = 0;
   for (const auto &l : launches) {
     CtrlView cv;
     int rc;
     if (l.size() == 1) {
-      const Pack &p = *l[0];
+      const UnionPack &p = l[0];
       grus_graph *g = b->graphs[p.graph];
       if (p.q.size() == 1) {
         const grus_query &q = queries[p.q[0]];
@@ -687,9 +639,9 @@ static int union_sssp(grus_batch *b, const grus_query *queries, const std::vecto
       std::vector<uint32_t> srcs;
       std::vector<uint32_t *> outs;
       for (size_t i = 0; i < l.size(); ++i) {
-        gs[i] = b->graphs[l[i]->graph];
-        kq[i] = (uint32_t)l[i]->q.size();
-        for (int qi : l[i]->q) {
+        gs[i] = b->graphs[l[i].graph];
+        kq[i] = (uint32_t)l[i].q.size();
+        for (int qi : l[i].q) {
           srcs.push_back(queries[qi].src);
           outs.push_back(out + queries[qi].out_offset);
         }
