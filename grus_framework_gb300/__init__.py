@@ -393,6 +393,8 @@ class Graph:
         _check(lib.grus_graph_save_gr(self._handle(), str(path).encode()), "grus_graph_save_gr")
 
     def set_tuning(self, **kw):
+        """Set fields of this graph's grus_tuning (the others keep their
+        values; 0 means the library default).  Unknown names raise TypeError."""
         t = Tuning()
         _check(lib.grus_graph_get_tuning(self._handle(), C.byref(t)), "grus_graph_get_tuning")
         known = {f for f, _ in t._fields_}
@@ -526,8 +528,13 @@ def _graph_array(graphs):
 
 
 class Batch:
-    """Many BFS / SSSP queries over several resident graphs in one launch
-    (cluster workers, include/grus.h grus_batch_*)."""
+    """Many BFS / SSSP queries over several resident graphs in one call
+    (include/grus.h grus_batch_*).  Queries on graphs of at least
+    `big_edges` edges run first as whole-GPU launches -- SSSP packs of up to
+    32 sources per graph, several graphs' packs per launch while their
+    distance rows total at most `launch_entries` entries -- and the rest on
+    cluster workers in one launch.  Zero arguments take the library
+    defaults (grus_batch_config)."""
 
     def __init__(self, graphs, cluster_size=0, workers=0, huge_degree=0, sssp_delta=0,
                  group_sources=0, big_edges=0, launch_entries=0):
