@@ -112,7 +112,8 @@ WORKLOADS = {
                                metric="GTEPS (single-query BFS, RMAT-26 symmetrised, managed "
                                       "memory, device budget 50% of the CSR bytes)"),
     "batch-sssp256": dict(algo="batch", graph="rmat-set", seed=4, queries=256, kernel="batch_kernel "
-                      "(cluster workers) + msssp_persistent (graphs of 2^21+ edges)",
+                      "(cluster workers) + msssp_persistent / msssp_union (graphs of 2^21+ "
+                      "edges, several per launch while their distance rows fit 2^23 entries)",
                       metric="queries/s (256 SSSP queries over 32 resident RMAT graphs, scales "
                              "14-20, edge factors 8-32, one batched call)"),
     "serve-mixed": dict(algo="serve", graph="rmat-set", seed=5, rate=8000, sweep_rates=[500, 2000],
