@@ -204,7 +204,7 @@ int msssp_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
   if (rc) return rc;
   GRUS_CUDA_TRY(cudaMemcpyAsync(w->srcs, hsrc, k * 4, cudaMemcpyHostToDevice, s));
   Args a;
-  std::memset(&a, 0, sizeof(a));
+  std::memset((void *)&a, 0, sizeof(a));
   a.v.offs = g->csr.offs;
   a.v.cols = g->csr.cols;
   a.v.wts = g->csr.wts;
