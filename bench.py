@@ -300,20 +300,26 @@ def msbfs_sources(n, offs_or_degree_fn, k, seed):
 def cpu_run(w, csr, csc, src, srcs, threads, budget_s=12.0, max_runs=5, nsrc=4):
     """Times the OpenMP version of the workload's algorithm on `threads` host
     threads (multi-source workloads: one run from each of the first `nsrc`
-    sources).  Returns (units per second, sample description)."""
+    sources).  Returns (units per second, sample description, results), the
+    results being what the runs computed, for the parity check of the GPU
+    output: {"rows": [(row, values), ...]} (row 0 for a single query, the
+    source's row for multi-source workloads) or {} for PageRank, whose bounded
+    sample runs fewer iterations than the GPU."""
     import oracle
     algo = w["algo"]
     times, units = [], 0
+    results = {}
     t_start = time.perf_counter()
     if algo in ("bfs", "sssp"):
         fn = oracle.omp_bfs if algo == "bfs" else oracle.omp_sssp
         d, _ = fn(csr, src, threads)
         units = oracle.reached_edges(csr, d)
+        results = {"rows": [(0, d)]}
         while len(times) < max_runs and (not times or time.perf_counter() - t_start < budget_s):
             times.append(fn(csr, src, threads)[1])
         desc = f"{len(times)} full {algo.upper()} runs from the source"
     elif algo == "cc":
-        oracle.omp_cc(csr, threads)
+        results = {"rows": [(0, oracle.omp_cc(csr, threads)[0])]}
         units = csr.m
         while len(times) < max_runs and (not times or time.perf_counter() - t_start < budget_s):
             times.append(oracle.omp_cc(csr, threads)[1])
@@ -329,15 +335,31 @@ def cpu_run(w, csr, csc, src, srcs, threads, budget_s=12.0, max_runs=5, nsrc=4):
     elif algo in ("msbfs", "msssp"):
         fn = oracle.omp_bfs if algo == "msbfs" else oracle.omp_sssp
         per = []
-        for s in srcs[:nsrc]:  # bounded sample: nsrc of the sources, one run each
+        results = {"rows": []}
+        for i, s in enumerate(srcs[:nsrc]):  # bounded sample: nsrc of the sources, one run each
             d, t = fn(csr, int(s), threads)
             per.append((oracle.reached_edges(csr, d), t))
+            results["rows"].append((i, d))
         units = sum(p[0] for p in per)
         times = [sum(p[1] for p in per)]
         desc = (f"one OpenMP {'BFS' if algo == 'msbfs' else 'SSSP'} from each of the first "
                 f"{min(nsrc, len(srcs))} of the {len(srcs)} sources")
     med = statistics.median(times)
-    return units / med / 1e9, f"{desc}, median {med*1e3:.1f} ms, OpenMP level-synchronous"
+    return units / med / 1e9, f"{desc}, median {med*1e3:.1f} ms, OpenMP level-synchronous", results
+
+
+def parity_entry(res, results, what):
+    """Compares rows of the GPU output `res` (1-D for one query, 2-D per
+    source) with the CPU port's results; the bench line carries the outcome."""
+    rows = results.get("rows", [])
+    if not rows:
+        return {"checked": "none in the bench (PageRank: tolerance tests in tests/)"}
+    bad = 0
+    for i, ref in rows:
+        got = res[i] if res.ndim == 2 else res
+        bad += int(np.count_nonzero(got.view(np.uint32) != ref))
+    return {"checked": f"{len(rows)} {what} of the timed configuration against the oracle's "
+                       "OpenMP port (bit-exact)", "mismatches": bad, "ok": bad == 0}
 
 
 def host_graph(w):
@@ -487,6 +509,7 @@ def run_grus(args, dist, rank, local):
     result = None
     if rank == 0:
         cpu = None
+        parity = {"checked": "skipped (--no-cpu-baseline)"}
         if not args.no_cpu_baseline:
             import oracle
             offs, cols, wts = g.copy_csr()
@@ -496,14 +519,16 @@ def run_grus(args, dist, rank, local):
                 co, cc_, _ = g.copy_csc()
                 csc = oracle.CSR(co, cc_)
             threads = host_threads()
-            v, sample = cpu_run(w, csr, csc, src, srcs, threads)
+            v, sample, cpu_results = cpu_run(w, csr, csc, src, srcs, threads)
             cpu = {"value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": sample}
+            parity = parity_entry(res, cpu_results,
+                                  "source rows" if algo in ("msbfs", "msssp") else "result")
             # the same port on one thread, one run (one source for multi-source;
             # skipped above 2^30 edges, where it would take minutes)
             if csr.m <= (1 << 30):
-                v1, sample1 = cpu_run(w, csr, csc, src, srcs, 1, budget_s=0.0, max_runs=1,
-                                      nsrc=1)
+                v1, sample1, _ = cpu_run(w, csr, csc, src, srcs, 1, budget_s=0.0, max_runs=1,
+                                         nsrc=1)
                 cpu["single_thread"] = {"value": round(v1, 4), "unit": UNIT, "cores": 1,
                                         "sample": sample1}
         clocks = clk.summary()
@@ -532,6 +557,7 @@ def run_grus(args, dist, rank, local):
                          "traffic_note": traffic_note, "peak_source": peak_kind,
                          "kernel": w["kernel"], "algorithmic_bytes_per_launch": alg},
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clocks,
         }
     g.free()
@@ -553,13 +579,16 @@ def sssp_or_bfs_bytes(algo_id, n, deg, d):
 
 def cpu_queries(graphs_host, queries, threads):
     """OpenMP BFS/SSSP of `queries` ((graph, algo, src) tuples) on host CSRs.
-    Returns (queries per second, total seconds)."""
+    Returns (queries per second, total seconds, the results in query order)."""
     import oracle
     total = 0.0
+    results = []
     for gi, algo_id, src in queries:
         fn = oracle.omp_sssp if algo_id == 1 else oracle.omp_bfs
-        total += fn(graphs_host[gi], int(src), threads)[1]
-    return len(queries) / total, total
+        d, t = fn(graphs_host[gi], int(src), threads)
+        total += t
+        results.append(d)
+    return len(queries) / total, total, results
 
 
 def roofline_entry(alg, seconds, traffic_key, kernel, note=None):
@@ -649,6 +678,7 @@ def run_batch(args, dist, rank, local):
     result = None
     if rank == 0:
         cpu = None
+        parity = {"checked": "skipped (--no-cpu-baseline)"}
         if not args.no_cpu_baseline:
             sample = queries[:16]
             hosts = {}
@@ -658,8 +688,13 @@ def run_batch(args, dist, rank, local):
                     o_, c_, wt_ = gs[gi].copy_csr()
                     hosts[gi] = oracle.CSR(o_, c_, wt_)
             threads = host_threads()
-            v, sec = cpu_queries(hosts, sample, threads)
-            v1, sec1 = cpu_queries(hosts, sample[:4], 1)
+            v, sec, cpu_res = cpu_queries(hosts, sample, threads)
+            v1, sec1, _ = cpu_queries(hosts, sample[:4], 1)
+            bad = sum(int(np.count_nonzero(res[off:off + gs[gi].n] != ref))
+                      for (gi, _, _), off, ref in zip(sample, layout, cpu_res))
+            parity = {"checked": f"the first {len(sample)} of the {nq} results against the "
+                                 "oracle's OpenMP port (bit-exact)", "mismatches": bad,
+                      "ok": bad == 0}
             cpu = {"value": round(v, 2), "unit": QPS, "cores": threads, "kind": "port",
                    "sample": f"OpenMP SSSP of the first {len(sample)} queries, {sec:.2f} s",
                    "single_thread": {"value": round(v1, 2), "unit": QPS, "cores": 1,
@@ -689,7 +724,7 @@ def run_batch(args, dist, rank, local):
                                            "device outputs, host clock"},
             "gpu_launches": launches * args.steps,
             "roofline": roofline_entry(alg, mean_ms * 1e-3, w["workload"], w["kernel"]),
-            "cpu_baseline": cpu, "clocks": clk.summary(),
+            "cpu_baseline": cpu, "parity": parity, "clocks": clk.summary(),
         }
     b.free()
     return result
@@ -813,6 +848,17 @@ def run_serve(args, dist, rank, local):
                       "p50_ms": round(float(np.percentile(lat, 50)) / 1e3, 3),
                       "p99_ms": round(float(np.percentile(lat, 99)) / 1e3, 3), "errors": int(err)})
         errors += err
+    # the parity sample: 12 queries of the mix served once more into their own
+    # outputs (compared below with the CPU port's results of the same queries)
+    check = plain[:12]
+    check_out = [torch.full((gs[gi].n,), -7, dtype=torch.int32, device="cuda") for gi, _, _ in check]
+    for j, (gi, algo_id, src) in enumerate(check):
+        srv.submit(gi, algo_id, src, check_out[j], 1 << 40 | j)
+    got_status = {}
+    t_chk = time.perf_counter()
+    while len(got_status) < len(check) and time.perf_counter() - t_chk < 60:
+        for tag, stt, _ in srv.poll(64, wait_ms=5):
+            got_status[tag] = stt
     srv.close()
     # algorithmic bytes of the timed queries: the mean per-query figure of the mix
     mean_q = sum((frac if a == grus.ALGO_SSSP else 1 - frac) * v / len(gs)
@@ -820,16 +866,23 @@ def run_serve(args, dist, rank, local):
     result = None
     if rank == 0:
         cpu = None
+        parity = {"checked": "skipped (--no-cpu-baseline)"}
         if not args.no_cpu_baseline:
             import oracle
-            sample = plain[:12]
+            sample = check
             hosts = {}
             for gi, _, _ in sample:
                 if gi not in hosts:
                     o_, c_, wt_ = gs[gi].copy_csr()
                     hosts[gi] = oracle.CSR(o_, c_, wt_)
             threads = host_threads()
-            v, sec = cpu_queries(hosts, sample, threads)
+            v, sec, cpu_res = cpu_queries(hosts, sample, threads)
+            bad = sum(int(np.count_nonzero(o.cpu().numpy().view(np.uint32) != ref))
+                      for o, ref in zip(check_out, cpu_res))
+            bad += sum(1 for stt in got_status.values() if stt != 0) + len(check) - len(got_status)
+            parity = {"checked": f"{len(check)} queries of the mix served into their own outputs "
+                                 "against the oracle's OpenMP port (bit-exact)",
+                      "mismatches": bad, "ok": bad == 0}
             cpu = {"value": round(v, 2), "unit": QPS, "cores": threads, "kind": "port",
                    "sample": f"OpenMP BFS/SSSP of {len(sample)} queries of the mix, {sec:.2f} s"}
         cfg = {"workload": w["workload"], "graphs": "RMAT scales 16-22 and 24, edge factor 16, "
@@ -861,7 +914,7 @@ def run_serve(args, dist, rank, local):
             "roofline": roofline_entry(int(mean_q * completed), secs, w["workload"], w["kernel"],
                                        note="all queries of the timed region: per query the "
                                             "BFS/SSSP figure of its graph, averaged over the mix"),
-            "cpu_baseline": cpu, "clocks": clk.summary(),
+            "cpu_baseline": cpu, "parity": parity, "clocks": clk.summary(),
         }
     return result
 
@@ -931,7 +984,7 @@ def run_reference(args, dist, rank):
     rates = []
     sample = ""
     for _ in range(args.steps):
-        r, sample = cpu_run(w, g, csc, src, srcs, threads, budget_s=0.0, max_runs=1)
+        r, sample, _ = cpu_run(w, g, csc, src, srcs, threads, budget_s=0.0, max_runs=1)
         rates.append(r)
     value = statistics.median(rates)
     cfg = {k_: v_ for k_, v_ in w.items() if k_ not in ("metric", "kernel")}
@@ -948,6 +1001,40 @@ def run_reference(args, dist, rank):
     }
 
 
+def systems_summary(args, dist, rank, local):
+    """The batched and served forms, measured in the same process after the
+    headline workload: one summary per form, for the default bench line."""
+    out = {}
+    for name, workload, fn in (("batch", "batch-sssp256", run_batch),
+                               ("serve", "serve-mixed", run_serve)):
+        a = argparse.Namespace(**vars(args))
+        a.workload, a.scale = workload, 0
+        r = fn(a, dist, rank, local)
+        if rank != 0 or r is None:
+            continue
+        plain = r["plain_back_to_back"]["value"]
+        e = {"workload": workload, "metric": r["metric"], "qps": r["value"],
+             "e2e_qps": r["e2e"]["value"], "plain_back_to_back_qps": plain,
+             "steps": r["steps"], "warmup": r["warmup"], "ms_per_step": r["ms_per_step"],
+             "gpu_launches": r["gpu_launches"], "parity": r.get("parity"),
+             "clocks": r.get("clocks")}
+        if name == "batch":
+            # host clock against host clock: the e2e rate (batched call plus
+            # every result copied to the host) over plain calls' rate
+            e["speedup_vs_plain"] = round(r["e2e"]["value"] / plain, 2)
+            e["speedup_note"] = ("e2e queries/s (host clock, results copied to the host) over "
+                                 "back-to-back plain grus_sssp calls (host clock)")
+        else:
+            e["speedup_vs_plain"] = round(r["value"] / plain, 2)
+            e["speedup_note"] = ("served queries/s over back-to-back plain calls of the same "
+                                 "mix, both on the host clock")
+            e["p50_ms"] = r["latency"]["p50_ms"]
+            e["p99_ms"] = r["latency"]["p99_ms"]
+            e["sweep"] = r.get("sweep")
+        out[name] = e
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -957,6 +1044,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--scale", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-systems", action="store_true",
+                    help="default workload only: skip the batched and served summaries")
     args = ap.parse_args()
     if args.impl == "grus":
         args.warmup = max(args.warmup, 3)
@@ -971,10 +1060,21 @@ def main():
         res = run_serve(args, dist, rank, local)
     else:
         res = run_grus(args, dist, rank, local)
+        if args.workload == DEFAULT_WORKLOAD and not args.scale and not args.no_systems:
+            sysres = systems_summary(args, dist, rank, local)
+            if rank == 0 and res is not None:
+                res["systems"] = sysres
+    failed = False
     if rank == 0 and res is not None:
         print(json.dumps(res))
+        checks = [res.get("parity")] + [v.get("parity") for v in res.get("systems", {}).values()]
+        failed = any(c is not None and c.get("ok") is False for c in checks)
+        if failed:
+            print("bench: GPU results differ from the oracle's (see \"parity\")", file=sys.stderr)
     if dist is not None:
         dist.destroy_process_group()
+    if failed:
+        sys.exit(3)
 
 
 if __name__ == "__main__":

@@ -135,6 +135,7 @@ def _load():
         "grus_save_result": ([C.c_char_p, vp, C.c_uint64, C.c_uint32], i32),
         "grus_telemetry_sample": ([C.POINTER(Telemetry)], i32),
         "grus_check_wait_limit": ([C.c_uint32], i32),
+        "grus_check_stale_barrier": ([vp, u32, u32, vp], i32),
         "grus_graph_from_csr": ([u64, u64, vp, vp, vp, u32, i32, u64, PG], i32),
         "grus_graph_load_gr": ([C.c_char_p, i32, i32, u64, PG], i32),
         "grus_graph_save_gr": ([vp, C.c_char_p], i32),
@@ -246,6 +247,19 @@ def check_wait_limit(timeout_ms: int = 100) -> int:
     """Runs the bounded-wait diagnostic (include/grus.h grus_check_wait_limit);
     returns its status code (ETIMEDOUT when the wait ended by its limit)."""
     return lib.grus_check_wait_limit(timeout_ms)
+
+
+CHECK_BFS, CHECK_SSSP, CHECK_BFS_MULTI, CHECK_SSSP_MULTI, CHECK_PAGERANK = 0, 1, 2, 3, 4
+
+
+def check_stale_barrier(g: "Graph", which: int, timeout_ms: int = 100, stream=None) -> None:
+    """Queues, without waiting, a one-CTA wait that times out on the control
+    block of `g`'s workspace for `which` (CHECK_*), leaving it as a launch that
+    timed out at a grid barrier leaves it (include/grus.h
+    grus_check_stale_barrier).  The next call on that workspace must still
+    run correctly."""
+    _check(lib.grus_check_stale_barrier(g._handle(), which, timeout_ms, _stream(stream)),
+           "grus_check_stale_barrier")
 
 
 def version() -> str:

@@ -909,6 +909,8 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   cfg.numAttrs = nattr;
 
   const bool sync = stats != nullptr || !dev_out;
+  // barrier and error word: a timed-out launch leaves stale barrier state
+  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffBar, 0, kOffSummary - kOffBar, s));
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
   GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a));
   // continues a long traversal the persistent kernel handed over; returns at
@@ -1017,27 +1019,60 @@ static_assert(kStaticBitmapOff % 256 == 0 && kStaticQueueOff % 256 == 0 &&
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
 std::mutex g_static_mu;
-void *g_static_base[64] = {};
-int g_static_occ = -1;
+// Per device: the context the entry was looked up in, the array's device
+// address in it and the persistent kernel's occupancy on that device.
+struct StaticEntry {
+  void *ctx = nullptr;
+  void *base = nullptr;
+  int occ = 0;
+};
+StaticEntry g_static[64];
 
-// Device address of g_static_scratch on the current device (looked up once).
-int static_scratch(void **base) {
+// The current CUDA context (cuCtxGetCurrent, reached through the runtime so
+// the library needs no link against the driver library), or null.
+void *current_context() {
+  using Fn = int (*)(void **);
+  static Fn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (Fn) nullptr;
+    return (Fn)p;
+  }();
+  void *ctx = nullptr;
+  if (fn && fn(&ctx) != 0) ctx = nullptr;
+  return ctx;
+}
+
+// Device address of g_static_scratch on the current device and the grid's
+// CTAs per SM.  Looked up once per device, and again if the device's context
+// changed since (a cudaDeviceReset makes the old address meaningless).
+int static_scratch(void **base, int *occ) {
   int dev = 0;
   GRUS_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return GRUS_ENODEV;
+  // the caller's pointer checks (cudaPointerGetAttributes) have made the
+  // device's context current by now
+  void *ctx = current_context();
   std::lock_guard<std::mutex> lk(g_static_mu);
-  if (!g_static_base[dev]) {
+  StaticEntry &e = g_static[dev];
+  if (!e.base || e.ctx != ctx) {
     void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (e != cudaSuccess || !p) {
-      set_last_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-      return status_from_cuda(e == cudaSuccess ? cudaErrorInvalidSymbol : e);
+    const cudaError_t rc = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (rc != cudaSuccess || !p) {
+      set_last_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(rc));
+      return status_from_cuda(rc == cudaSuccess ? cudaErrorInvalidSymbol : rc);
     }
-    g_static_base[dev] = p;
+    int o = 0;
+    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, bfs_persistent<4>, kBlock, 0));
+    e.ctx = ctx;
+    e.base = p;
+    e.occ = std::max(o, 1);
   }
-  if (g_static_occ < 0)
-    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_static_occ, bfs_persistent<4>, kBlock, 0));
-  *base = g_static_base[dev];
+  *base = e.base;
+  *occ = e.occ;
   return GRUS_OK;
 }
 
@@ -1063,7 +1098,8 @@ extern "C" int grus_bfs_static(uint64_t n, uint64_t m, const uint32_t *offsets,
   }
   cudaStream_t s = (cudaStream_t)stream;
   void *base = nullptr;
-  int rc = static_scratch(&base);
+  int occ = 1;
+  int rc = static_scratch(&base, &occ);
   if (rc) return rc;
   char *ctrl = (char *)base;
   uint32_t *bitmaps = (uint32_t *)((char *)base + kStaticBitmapOff);
@@ -1110,7 +1146,7 @@ extern "C" int grus_bfs_static(uint64_t n, uint64_t m, const uint32_t *offsets,
   attr.id = cudaLaunchAttributeCooperative;
   attr.val.cooperative = 1;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(device_sm_count() * std::max(g_static_occ, 1)));
+  cfg.gridDim = dim3((unsigned)(device_sm_count() * occ));
   cfg.blockDim = dim3(kBlock);
   cfg.stream = s;
   cfg.attrs = &attr;
@@ -1142,6 +1178,7 @@ CtrlView bfs_ctrl(grus_graph *g) {
     v.ctrl = w->ctrl;
     v.bytes = kCtrlBytes;
     v.err_off = kOffErr;
+    v.bar_off = kOffBar;
   }
   return v;
 }

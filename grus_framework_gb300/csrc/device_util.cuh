@@ -17,6 +17,8 @@ enum : uint32_t {
   kErrTimeout = 1u << 0,   // a grid-barrier wait ran past its limit
   kErrOverflow = 1u << 1,  // a queue or chunk list would have overflowed
   kErrLevels = 1u << 2,    // level counter passed its bound
+  kErrAborted = 1u << 3,   // a CTA left a grid barrier because another CTA's
+                           // wait had run past its limit
 };
 
 // ---- device helpers ------------------------------------------------------
@@ -61,7 +63,12 @@ __device__ __forceinline__ uint32_t agg_reserve(uint32_t *counter) {
 
 // Grid barrier for cooperative (co-resident) launches.  Every wait is
 // bounded: past `timeout_ns` the waiting CTA raises the shared abort flag and
-// kErrTimeout, and every CTA then returns false so the kernel exits cleanly.
+// kErrTimeout, and every CTA then returns false so the kernel exits cleanly;
+// a CTA that leaves because it saw the flag adds kErrAborted, so a launch cut
+// short never reads as a success.  A launch that timed out leaves the flag
+// and a stale arrival count behind, so the host clears the barrier and the
+// error word in the launch's stream before every launch on them (a stale
+// count would otherwise let a later episode complete early).
 struct GridBarrier {
   uint32_t count;
   uint32_t gen;
@@ -86,7 +93,11 @@ __device__ __forceinline__ bool grid_sync(GridBarrier *bar, uint32_t *err,
       const uint64_t t0 = global_timer_ns();
       uint32_t spins = 0;
       while (ld_acquire_u32(&bar->gen) == gen) {
-        if (ld_acquire_u32(&bar->abort)) { ok = 0; break; }
+        if (ld_acquire_u32(&bar->abort)) {
+          atomicOr(err, kErrAborted);
+          ok = 0;
+          break;
+        }
         __nanosleep(40);
         if ((++spins & 255u) == 0 && global_timer_ns() - t0 > timeout_ns) {
           atomicExch(&bar->abort, 1u);

@@ -37,6 +37,10 @@ int status_from_device_error(uint32_t bits) {
     set_last_error("a device-side wait exceeded its time limit");
     return GRUS_ETIMEDOUT;
   }
+  if (bits & kErrAborted) {
+    set_last_error("the launch was abandoned at a grid barrier after a wait timed out");
+    return GRUS_ETIMEDOUT;
+  }
   if (bits & (kErrOverflow | kErrLevels)) {
     set_last_error("a device queue or level bound overflowed");
     return GRUS_EOVERFLOW;
@@ -170,6 +174,19 @@ __global__ void k_max_degree(const uint32_t *__restrict__ offs, uint64_t n,
 // One CTA enters the persistent kernels' grid barrier; the host presets its
 // arrival count so the episode cannot complete and the wait must time out.
 __global__ void k_wait_limit(GridBarrier *bar, uint32_t *err, uint64_t timeout_ns) {
+  grid_sync(bar, err, timeout_ns);
+}
+
+// The same one-CTA wait on a workspace's own control block: the CTA first
+// counts one phantom arrival, so its wait must time out, and the block is
+// left as a launch that timed out leaves it (abort raised, arrival count
+// stale, error word set).
+__global__ void k_stale_barrier(GridBarrier *bar, uint32_t *err, uint64_t timeout_ns) {
+  if (threadIdx.x == 0) {
+    bar->count = 1u;
+    bar->abort = 0u;
+    __threadfence();
+  }
   grid_sync(bar, err, timeout_ns);
 }
 
@@ -480,6 +497,29 @@ int grus_check_wait_limit(uint32_t timeout_ms) {
   }
   set_last_error("device wait did not report its time limit");
   return GRUS_ECUDA;
+}
+
+int grus_check_stale_barrier(grus_graph *g, uint32_t which, uint32_t timeout_ms, void *stream) {
+  if (!g || timeout_ms < 1 || timeout_ms > 10000) return GRUS_EINVAL;
+  CtrlView v;
+  switch (which) {
+    case GRUS_CHECK_BFS: v = bfs_ctrl(g); break;
+    case GRUS_CHECK_SSSP: v = sssp_ctrl(g); break;
+    case GRUS_CHECK_BFS_MULTI: v = msbfs_ctrl(g); break;
+    case GRUS_CHECK_SSSP_MULTI: v = msssp_ctrl(g); break;
+    case GRUS_CHECK_PAGERANK: v = pr_ctrl(g); break;
+    default: return GRUS_EINVAL;
+  }
+  if (!v.ctrl) {
+    set_last_error("the graph has no workspace for this algorithm yet (run it once first)");
+    return GRUS_EINVAL;
+  }
+  GRUS_CUDA_TRY(cudaSetDevice(g->device));
+  k_stale_barrier<<<1, 32, 0, (cudaStream_t)stream>>>((GridBarrier *)(v.ctrl + v.bar_off),
+                                                       (uint32_t *)(v.ctrl + v.err_off),
+                                                       (uint64_t)timeout_ms * 1000000ull);
+  GRUS_CUDA_TRY(cudaGetLastError());
+  return GRUS_OK;
 }
 
 int grus_graph_from_csr(uint64_t n, uint64_t m, const uint32_t *offsets,

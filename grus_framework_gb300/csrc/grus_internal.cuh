@@ -104,12 +104,13 @@ inline uint32_t bfs_pack_min(uint64_t m) {
 // without waiting and check the launch's error word later.
 struct CtrlView {
   char *ctrl = nullptr;
-  size_t bytes = 0, err_off = 0;
+  size_t bytes = 0, err_off = 0, bar_off = 0;
 };
 CtrlView bfs_ctrl(grus_graph *g);
 CtrlView sssp_ctrl(grus_graph *g);
 CtrlView msbfs_ctrl(grus_graph *g);
 CtrlView msssp_ctrl(grus_graph *g);
+CtrlView pr_ctrl(grus_graph *g);
 
 // Multi-graph multi-source SSSP (msssp.cu): ONE whole-GPU launch over ng
 // (<= 64) weighted graphs, graph g with kq[g] (1..32) sources; srcs and outs

@@ -511,7 +511,8 @@ int msbfs_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
   a.summary = (Summary *)(w->ctrl + kOffSummary);
   a.alpha = tune_or(g->tuning.multi_alpha, k > 32 ? kDefAlphaWide : kDefAlpha);
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
-  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffSummary, 0, kCtrlBytes - kOffSummary, s));
+  // barrier, error word and summary: a timed-out launch leaves stale barrier state
+  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffBar, 0, kCtrlBytes - kOffBar, s));
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
   void *args[] = {&a};
   rc = launch_persistent((const void *)msbfs_persistent, args, kBlock, (int)g->tuning.ctas_per_sm,
@@ -594,6 +595,7 @@ CtrlView msbfs_ctrl(grus_graph *g) {
     v.ctrl = w->ctrl;
     v.bytes = kCtrlBytes;
     v.err_off = kOffErr;
+    v.bar_off = kOffBar;
   }
   return v;
 }

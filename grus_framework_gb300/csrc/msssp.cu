@@ -226,7 +226,8 @@ int msssp_run(grus_graph *g, const uint32_t *hsrc, int k, uint32_t *const *outs,
   a.bar = (GridBarrier *)(w->ctrl + kOffBar);
   a.summary = (Summary *)(w->ctrl + kOffSummary);
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
-  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffSummary, 0, kCtrlBytes - kOffSummary, s));
+  // barrier, error word and summary: a timed-out launch leaves stale barrier state
+  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffBar, 0, kCtrlBytes - kOffBar, s));
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
   // row width must match the kernel: a workspace sized for a wider row is
   // used at its own width
@@ -388,7 +389,7 @@ int msssp_union_run(void *wsp, int region, grus_graph *const *gs, int ng, const 
   GRUS_CUDA_TRY(cudaMemcpyAsync(ugd, ugh, ng * sizeof(ms::UnionGraph), cudaMemcpyHostToDevice, s));
   GRUS_CUDA_TRY(cudaMemcpyAsync(sd, sv, nseeds * 4, cudaMemcpyHostToDevice, s));
   GRUS_CUDA_TRY(cudaMemcpyAsync(sd + kSeedCap, ss, nseeds * 4, cudaMemcpyHostToDevice, s));
-  GRUS_CUDA_TRY(cudaMemsetAsync(ctrl + kOffSummary, 0, kCtrlBytes - kOffSummary, s));
+  GRUS_CUDA_TRY(cudaMemsetAsync(ctrl + kOffBar, 0, kCtrlBytes - kOffBar, s));
   UnionArgs a;
   std::memset((void *)&a, 0, sizeof(a));
   a.v.n = (uint32_t)V;
@@ -467,6 +468,7 @@ CtrlView msssp_ctrl(grus_graph *g) {
     v.ctrl = w->ctrl;
     v.bytes = kCtrlBytes;
     v.err_off = kOffErr;
+    v.bar_off = kOffBar;
   }
   return v;
 }

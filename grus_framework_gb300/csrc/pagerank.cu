@@ -387,7 +387,9 @@ extern "C" int grus_pagerank(grus_graph *g, float damping, int iters, float *ran
     GRUS_CUDA_TRY(cudaStreamSynchronize(s));
     return GRUS_OK;
   }
-  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffHeavy, 0, 8, s));  // heavy-list counters
+  // barrier, error word and heavy-list counters: a timed-out launch leaves
+  // stale barrier state
+  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffBar, 0, kOffHeavy + 8 - kOffBar, s));
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
   void *args[] = {&a};
   rc = launch_persistent((const void *)pr_persistent, args, kBlock, (int)g->tuning.ctas_per_sm,
@@ -416,3 +418,18 @@ extern "C" int grus_pagerank(grus_graph *g, float damping, int iters, float *ran
   }
   return GRUS_OK;
 }
+
+namespace grus {
+CtrlView pr_ctrl(grus_graph *g) {
+  CtrlView v;
+  std::lock_guard<std::mutex> lk(g->mu);
+  const Workspace *w = (const Workspace *)g->ws[kWsPr];
+  if (w) {
+    v.ctrl = w->ctrl;
+    v.bytes = kCtrlBytes;
+    v.err_off = kOffErr;
+    v.bar_off = kOffBar;
+  }
+  return v;
+}
+}  // namespace grus

@@ -354,7 +354,8 @@ extern "C" int grus_sssp(grus_graph *g, uint32_t src, uint32_t *dist,
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
 
   const bool sync = stats != nullptr || !dev_out;
-  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffSummary, 0, kCtrlBytes - kOffSummary, s));
+  // barrier, error word and summary: a timed-out launch leaves stale barrier state
+  GRUS_CUDA_TRY(cudaMemsetAsync(w->ctrl + kOffBar, 0, kCtrlBytes - kOffBar, s));
   if (stats) GRUS_CUDA_TRY(cudaEventRecord(w->ev0, s));
   void *args[] = {&a};
   rc = launch_persistent((const void *)sssp_persistent, args, kBlock,
@@ -416,6 +417,7 @@ CtrlView sssp_ctrl(grus_graph *g) {
     v.ctrl = w->ctrl;
     v.bytes = kCtrlBytes;
     v.err_off = kOffErr;
+    v.bar_off = kOffBar;
   }
   return v;
 }

@@ -11,8 +11,9 @@
 // expansion of csrc/expand.cuh:
 //   * a tile of 256 sources is expanded with CTA (degree >= 256), warp
 //     (>= 32) and scan-based gather (< 32) mappings, coalesced column loads;
-//   * sources of degree >= 8192 are cut into 4096-edge pieces and expanded by
-//     a second launch, one piece per CTA, so hubs spread over every SM.
+//   * sources of degree >= 8192 are cut into 1024-edge pieces (grus::kChunk)
+//     and expanded by a second launch, one piece per CTA, so hubs spread over
+//     every SM.
 // kernel<..., Frontier<BDF>> calls job.prepare() before each launch, as the
 // reference does; kernel_pull does not (the reference's kernel_pull never
 // calls it, kernel.cuh:128-133, and the pull samples are written for that).

@@ -129,6 +129,22 @@ GRUS_API int grus_device_init(int device);
  * Returns GRUS_ETIMEDOUT after about timeout_ms (1..10000) with the device
  * context still usable, or another status if the wait did not behave. */
 GRUS_API int grus_check_wait_limit(uint32_t timeout_ms);
+/* Diagnostic of the barrier reset between launches, no counterpart in the
+ * reference: queues on `stream`, without waiting, the same one-CTA wait on
+ * the control block of one of the graph's workspaces (`which`, below; the
+ * workspace exists once that algorithm has run on the graph), so the block
+ * is left as a launch that timed out at a grid barrier leaves it: abort flag
+ * raised, arrival count stale, error word set.  Every launch clears its
+ * block's barrier and error word in its own stream first, so a call queued
+ * behind this one runs normally.  Returns GRUS_OK once queued, GRUS_EINVAL
+ * when the workspace does not exist or timeout_ms is outside 1..10000. */
+#define GRUS_CHECK_BFS 0u
+#define GRUS_CHECK_SSSP 1u
+#define GRUS_CHECK_BFS_MULTI 2u
+#define GRUS_CHECK_SSSP_MULTI 3u
+#define GRUS_CHECK_PAGERANK 4u
+GRUS_API int grus_check_stale_barrier(grus_graph *g, uint32_t which, uint32_t timeout_ms,
+                                      void *stream);
 
 /* ---- graphs -------------------------------------------------------------- */
 /* CSR from host arrays.  Replaces graph_t<CSR> filled by
@@ -217,10 +233,17 @@ GRUS_API int grus_sssp_trace(grus_graph *g, grus_level_trace *out, int max_level
  * in-edges, else the BFS runs push-only) with its scratch in a fixed
  * file-scope device array held by every GPU that loads the library (about
  * 10 MB).  Graphs above the limits below are rejected with GRUS_EOVERFLOW.
- * The first call on a device looks the array up (make it before any stream
- * capture).  All calls share the array: calls that overlap on the GPU race.
- * Asynchronous on `stream` unless `stats` is given (then it waits and reports
- * device-side errors). */
+ * The arrays must form a valid CSR: offsets[0] == 0, offsets monotone,
+ * offsets[n] == m and every cols entry < n.  This is NOT checked (the arrays
+ * stay on the device); a column id >= n makes the kernel write past the
+ * depth array and past its own scratch, which later calls on that GPU share.
+ * The first call on a device (and the first after a cudaDeviceReset) looks
+ * the array up; make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race.  Asynchronous on `stream` unless
+ * `stats` is given; then it waits and reports device-side errors (a grid
+ * barrier that timed out).  With stats == NULL such errors are dropped: the
+ * next call clears the control block before anyone reads it, so callers who
+ * need them must pass stats, which makes the call synchronous. */
 #define GRUS_STATIC_MAX_VERTICES (1u << 20)
 #define GRUS_STATIC_MAX_EDGES (1u << 25)
 GRUS_API int grus_bfs_static(uint64_t n, uint64_t m, const uint32_t *offsets,

@@ -20,6 +20,8 @@ ROOT = HERE.parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
 LIB = BUILD / "libgrus_oracle.so"
+# The Grus source tree, read in place (never copied): GRUS_REFERENCE, else the
+# build container's checkout.  Absent on the GPU machine, where the pin is skipped.
 REF_SRC = Path(os.environ.get("GRUS_REFERENCE", "/root/reference"))
 
 

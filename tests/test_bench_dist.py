@@ -72,6 +72,26 @@ def test_query_workload_helpers():
     rng = np.random.default_rng(5)
     srcs = [bench.draw_source(rng, g.offs) for _ in range(50)]
     assert all(g.offs[v + 1] > g.offs[v] for v in srcs)
-    qps, sec = bench.cpu_queries({0: g}, [(0, 1, srcs[0]), (0, 0, srcs[1])], 2)
+    qps, sec, res = bench.cpu_queries({0: g}, [(0, 1, srcs[0]), (0, 0, srcs[1])], 2)
     assert qps > 0 and sec > 0
+    # the results the bench's parity check compares against: the oracle's
+    assert np.array_equal(res[0], oracle.sssp(g, srcs[0]))
+    assert np.array_equal(res[1], oracle.bfs(g, srcs[1]))
+
+
+def test_parity_entry_counts_mismatches():
+    sys.path.insert(0, str(ROOT))
+    import numpy as np
+    import bench
+    ref = np.arange(10, dtype=np.uint32)
+    ok = bench.parity_entry(ref.copy(), {"rows": [(0, ref)]}, "result")
+    assert ok["ok"] and ok["mismatches"] == 0
+    bad = ref.copy()
+    bad[3] = 99
+    e = bench.parity_entry(bad, {"rows": [(0, ref)]}, "result")
+    assert not e["ok"] and e["mismatches"] == 1
+    two = np.stack([ref, bad])
+    e2 = bench.parity_entry(two, {"rows": [(0, ref), (1, ref)]}, "source rows")
+    assert e2["mismatches"] == 1
+    assert "none" in bench.parity_entry(ref, {}, "result")["checked"]
 

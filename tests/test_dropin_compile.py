@@ -14,7 +14,7 @@ import sys
 sys.path.insert(0, str(Path(__file__).resolve().parent / "dropin"))
 import build_apps  # noqa: E402
 
-REF = Path(os.environ.get("GRUS_REFERENCE", "/root/reference"))
+from oracle.build import REF_SRC as REF  # noqa: E402  (GRUS_REFERENCE: the Grus source tree)
 SAMPLES = ["bfs", "sssp", "cc", "pagerank", "bfs_2s"]
 
 

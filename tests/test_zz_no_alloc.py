@@ -5,9 +5,11 @@ owns the whole device budget through its own pool, or loops that cannot
 afford cudaMalloc's device-wide synchronisation): its scratch is a fixed
 device array inside libgrus, and the caller passes device CSR arrays and a
 device output.  This file checks, through the C ABI, that two calls in a row
-give exactly the depths of the allocating entry point grus_bfs (bit-exact,
-the bar of every BFS test here), for a symmetric graph (direction-optimising)
-and a directed one (push only), and that oversized graphs are refused.
+give exactly the depths of the allocating entry point grus_bfs and of the
+oracle (bit-exact, the bar of every BFS test here), for a symmetric graph
+(direction-optimising) and a directed one (push only), that an asynchronous
+call followed by a synchronous one gives exact depths for both, and that
+oversized graphs are refused.
 It is collected last so that a run stopping at the first failure has run
 every other test first; it passes alone in a fresh process as well.
 """
@@ -28,10 +30,12 @@ def _static_fn(grus):
 
 
 @pytest.mark.parametrize("symmetric", [True, False])
-def test_static_bfs_matches_grus_bfs_twice(grus, symmetric):
+def test_static_bfs_matches_grus_bfs_twice(grus, oracle_mod, symmetric):
     torch = pytest.importorskip("torch")
     fn = _static_fn(grus)
     g = grus.Graph.rmat(16, 16, 1, symmetric=symmetric)
+    offs, cols, _ = g.copy_csr()
+    csr = oracle_mod.CSR(offs, cols)
     info = g.info()
     assert info.n <= (1 << 20) and info.m <= (1 << 25)
     out = torch.empty(info.n, dtype=torch.int32, device="cuda")
@@ -44,22 +48,34 @@ def test_static_bfs_matches_grus_bfs_twice(grus, symmetric):
         assert rc == 0, grus.lib.grus_last_error()
         got = out.cpu().numpy().view(np.uint32)
         assert np.array_equal(got, ref)
+        assert np.array_equal(got, oracle_mod.bfs(csr, src))
         assert st.vertices_reached == ref_st["vertices_reached"]
         assert st.edges_reached == ref_st["edges_reached"]
     g.free()
 
 
-def test_static_bfs_async_then_sync(grus):
-    """Without stats the call is asynchronous on the stream; results match."""
+def test_static_bfs_async_then_sync(grus, oracle_mod):
+    """Without stats the call is asynchronous on the stream; a call with
+    stats queued right behind it on the same stream (and the same shared
+    scratch) reports success, and both give exact depths."""
     torch = pytest.importorskip("torch")
     fn = _static_fn(grus)
     g = grus.Graph.rmat(14, 8, 3, symmetric=True)
+    offs, cols, _ = g.copy_csr()
+    csr = oracle_mod.CSR(offs, cols)
     info = g.info()
     out = torch.empty(info.n, dtype=torch.int32, device="cuda")
+    out2 = torch.empty(info.n, dtype=torch.int32, device="cuda")
     s = torch.cuda.Stream()
     rc = fn(info.n, info.m, info.offsets, info.cols, 1, 7, out.data_ptr(), None, s.cuda_stream)
     assert rc == 0
+    st = grus.Stats()
+    rc = fn(info.n, info.m, info.offsets, info.cols, 1, 11, out2.data_ptr(), C.byref(st),
+            s.cuda_stream)
+    assert rc == 0, grus.lib.grus_last_error()
     s.synchronize()
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), oracle_mod.bfs(csr, 7))
+    assert np.array_equal(out2.cpu().numpy().view(np.uint32), oracle_mod.bfs(csr, 11))
     assert np.array_equal(out.cpu().numpy().view(np.uint32), grus.bfs(g, 7))
 
 
