@@ -3,21 +3,28 @@
 // kernel_pull<>, job/updater/generator/pull_selector functors, SaveResults).
 // Each mode runs one operator and writes "<i> <value>" lines to --output.
 //
-//   apps --algo=bfs|sssp|cc|pr --input=g.gr --src=S --output=out.txt
-//        [--pull] [--frontier=bdf|wl|auto|bitmap]
+//   apps --algo=bfs|sssp|cc|pr|bfs2s --input=g.gr --src=S --output=out.txt
+//        [--pull] [--frontier=bdf|wl|auto|bitmap] [--mem=managed --budget=X]
+//
+// bfs2s is the two-stage active-subgraph BFS: Frontier_2S<BDF>, two
+// Subgraph<NORMAL> swapped every level and kernel_2s, driven the way the
+// reference's bfs_2s sample drives them (samples/bfs_2s/bfs_2s.cu:94-138).
 #include <gflags/gflags.h>
 
 #include "app.cuh"
 #include "common.cuh"
 #include "frontier.cuh"
+#include "frontier_2s.cuh"
 #include "graph.cuh"
 #include "graph_loader.cuh"
 #include "kernel.cuh"
+#include "kernel_2s.cuh"
+#include "subgraph.cuh"
 #include "worklist.cuh"
 
 using namespace mgg;
 
-DEFINE_string(algo, "bfs", "bfs | sssp | cc | pr");
+DEFINE_string(algo, "bfs", "bfs | sssp | cc | pr | bfs2s");
 DEFINE_string(frontier, "bdf", "push frontier: bdf | wl | auto | bitmap");
 
 namespace t {
@@ -174,6 +181,28 @@ uint run_pull(graph_t<CSR> &Gcsr, job_t &job, bool full) {
   return job.itr;
 }
 
+// Two-stage BFS: each level expands the frontier's "local" vertices over the
+// subgraph built one level earlier and gathers the rows of its "remote"
+// vertices into a fresh subgraph before expanding them; the two subgraphs
+// trade places every level.
+uint run_bfs_2s(graph_t<CSR> &G, job_t &job) {
+  frontier::Frontier_2S<BDF> F;
+  F.Init(G.numNode, FLAGS_src, FLAGS_device, 1.0, false);
+  Subgraph<NORMAL> SG1, SG2;
+  SG1.reserve(G.numNode, G.numEdge);
+  SG2.reserve(G.numNode, G.numEdge);
+  Subgraph<NORMAL> *SG_local = &SG1, *SG_remote = &SG2;
+  kernel_2s<graph_t<CSR>, Subgraph<NORMAL>, frontier::Frontier_2S<BDF>, bfs_update, mark, job_t> K;
+  while (!F.finish()) {
+    K(G, *SG_local, *SG_remote, F, job);
+    H_ERR(cudaDeviceSynchronize());
+    std::swap(SG_local, SG_remote);
+    F.Next();
+    job.itr++;
+  }
+  return job.itr;
+}
+
 bool Single() {
   H_ERR(cudaSetDevice(FLAGS_device));
   graph_t<CSR> G(FLAGS_algo == "sssp");
@@ -205,7 +234,9 @@ bool Single() {
   else fill<<<n / BLOCK_SIZE + 1, BLOCK_SIZE>>>(job.label, n, INFINIT, FLAGS_src, 0);
   if (FLAGS_algo == "sssp") job.adjwgt = G.adjwgt;
   const bool full = FLAGS_algo == "cc";
-  if (FLAGS_pull) {
+  if (FLAGS_algo == "bfs2s") {
+    itr = run_bfs_2s(G, job);
+  } else if (FLAGS_pull) {
     if (FLAGS_algo == "bfs") itr = run_pull<bfs_update, bfs_unvisited>(G, job, full);
     else if (FLAGS_algo == "sssp") itr = run_pull<sssp_update, any_vertex>(G, job, full);
     else itr = run_pull<cc_update, any_vertex>(G, job, full);

@@ -99,3 +99,31 @@ def test_dropin_delta_pagerank(apps, tmp_path, rmat_gr, oracle_mod):
     ref, _ = oracle_mod.delta_pagerank(g)
     rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-12)
     assert rel.mean() < 1e-3 and rel.max() < 1e-2, (rel.mean(), rel.max())
+
+
+# The two-stage active-subgraph BFS (the reference's bfs_2s: Frontier_2S<BDF>,
+# Subgraph<NORMAL>, kernel_2s): every level gathers the frontier's rows into a
+# compact subgraph on the device and expands over it.  Depths bit-exact
+# against the oracle, with the CSR in HBM and in managed memory under half the
+# CSR bytes as device budget.
+MEM_MODES = [(), ("--mem=managed", "--budget=0.5")]
+
+
+@pytest.mark.parametrize("mem", MEM_MODES)
+@pytest.mark.parametrize("kind", ["sym", "dir"])
+def test_dropin_bfs_2s(apps, tmp_path, rmat_gr, oracle_mod, kind, mem):
+    p, g = rmat_gr[kind]
+    deg = np.diff(g.offs.astype(np.int64))
+    for src in (oracle_mod.max_degree_vertex(g), int(np.flatnonzero(deg > 0)[7])):
+        got = np.array(run(apps, tmp_path, p, "bfs2s", src, mem), np.uint64)
+        assert np.array_equal(got, oracle_mod.bfs(g, src).astype(np.uint64)), src
+
+
+@pytest.mark.parametrize("mem", MEM_MODES)
+def test_dropin_bfs_2s_golden_fixtures(apps, tmp_path, mem):
+    import json
+    ans = json.loads((GOLDEN / "known_answers.json").read_text())
+    for name, a in ans.items():
+        for s, exp in a["bfs"].items():
+            got = [int(x) for x in run(apps, tmp_path, GOLDEN / f"{name}.gr", "bfs2s", int(s), mem)]
+            assert got == exp, name
