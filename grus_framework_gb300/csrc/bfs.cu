@@ -152,8 +152,11 @@ struct Workspace {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
-constexpr size_t kOffSlots = 0, kOffBar = 256, kOffErr = 320, kOffSummary = 384,
-                 kOffHandover = 448, kCtrlBytes = 512;
+constexpr size_t kOffSlots = 0, kOffBar = 256, kOffErr = 512, kOffSummary = 576,
+                 kOffHandover = 640, kCtrlBytes = 768;
+static_assert(kOffBar % 128 == 0 && kOffBar + sizeof(GridBarrier) <= kOffErr, "barrier layout");
+static_assert(4 * sizeof(LevelSlot) <= kOffBar && sizeof(Summary) <= kOffHandover - kOffSummary,
+              "control block layout");
 static_assert(kOffHandover + sizeof(Handover) <= kCtrlBytes, "hand-over overflows the control block");
 
 void ws_free(void *p) {

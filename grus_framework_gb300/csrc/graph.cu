@@ -471,21 +471,23 @@ int grus_device_init(int device) {
 
 int grus_check_wait_limit(uint32_t timeout_ms) {
   if (timeout_ms < 1 || timeout_ms > 10000) return GRUS_EINVAL;
+  constexpr size_t kErrOff = sizeof(GridBarrier), kBytes = kErrOff + 64;
   char *ctrl = nullptr;
-  GRUS_CUDA_TRY(cudaMalloc(&ctrl, 64));
-  // barrier at offset 0, error word at 32; one arrival already counted, so
+  GRUS_CUDA_TRY(cudaMalloc(&ctrl, kBytes));
+  // barrier at offset 0, error word after it; one arrival already counted, so
   // the single CTA of the launch never sees the episode complete
-  GridBarrier preset{1u, 0u, 0u, 0u};
-  cudaError_t e = cudaMemset(ctrl, 0, 64);
+  GridBarrier preset{};
+  preset.count = 1u;
+  cudaError_t e = cudaMemset(ctrl, 0, kBytes);
   if (e == cudaSuccess) e = cudaMemcpy(ctrl, &preset, sizeof(preset), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
-    k_wait_limit<<<1, 32>>>((GridBarrier *)ctrl, (uint32_t *)(ctrl + 32),
+    k_wait_limit<<<1, 32>>>((GridBarrier *)ctrl, (uint32_t *)(ctrl + kErrOff),
                             (uint64_t)timeout_ms * 1000000ull);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   uint32_t err = 0;
-  if (e == cudaSuccess) e = cudaMemcpy(&err, ctrl + 32, 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&err, ctrl + kErrOff, 4, cudaMemcpyDeviceToHost);
   cudaFree(ctrl);
   if (e != cudaSuccess) {
     set_last_error(cudaGetErrorString(e));

@@ -403,7 +403,10 @@ struct Workspace {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
-constexpr size_t kOffSlots = 0, kOffBar = 256, kOffErr = 320, kOffSummary = 384, kCtrlBytes = 512;
+constexpr size_t kOffSlots = 0, kOffBar = 256, kOffErr = 512, kOffSummary = 576, kCtrlBytes = 768;
+static_assert(kOffBar % 128 == 0 && kOffBar + sizeof(GridBarrier) <= kOffErr, "barrier layout");
+static_assert(4 * sizeof(Slot) <= kOffBar && sizeof(Summary) <= kCtrlBytes - kOffSummary,
+              "control block layout");
 
 void ws_free(void *p) {
   Workspace *w = (Workspace *)p;

@@ -118,8 +118,9 @@ struct Workspace {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
-constexpr size_t kOffSlots = 0, kOffFar = 256, kOffBar = 320, kOffErr = 384, kOffSummary = 448,
-                 kCtrlBytes = 512;
+constexpr size_t kOffSlots = 0, kOffFar = 256, kOffBar = 384, kOffErr = 640, kOffSummary = 704,
+                 kCtrlBytes = 768;
+static_assert(kOffBar % 128 == 0 && kOffBar + sizeof(GridBarrier) <= kOffErr, "barrier layout");
 static_assert(4 * sizeof(Slot) <= kOffFar, "slots overlap the far control");
 static_assert(sizeof(Summary) <= kCtrlBytes - kOffSummary, "summary overflows the control block");
 

@@ -291,7 +291,8 @@ struct Workspace {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
-constexpr size_t kOffBar = 0, kOffErr = 64, kOffHeavy = 96, kCtrlBytes = 128;
+constexpr size_t kOffBar = 0, kOffErr = 256, kOffHeavy = 320, kCtrlBytes = 384;
+static_assert(kOffBar + sizeof(GridBarrier) <= kOffErr, "barrier layout");
 
 void ws_free(void *p) {
   Workspace *w = (Workspace *)p;

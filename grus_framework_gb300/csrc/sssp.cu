@@ -100,8 +100,12 @@ struct Workspace {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
-constexpr size_t kOffSlots = 0, kOffFar = 256, kOffBar = 320, kOffErr = 384,
-                 kOffSummary = 448, kCtrlBytes = 512;
+constexpr size_t kOffSlots = 0, kOffFar = 256, kOffBar = 384, kOffErr = 640,
+                 kOffSummary = 704, kCtrlBytes = 768;
+static_assert(kOffBar % 128 == 0 && kOffBar + sizeof(GridBarrier) <= kOffErr, "barrier layout");
+static_assert(4 * sizeof(Slot) <= kOffFar && sizeof(FarCtl) <= kOffBar - kOffFar &&
+                  sizeof(Summary) <= kCtrlBytes - kOffSummary,
+              "control block layout");
 
 void ws_free(void *p) {
   Workspace *w = (Workspace *)p;
