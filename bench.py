@@ -624,7 +624,17 @@ def run_batch(args, dist, rank, local):
     for i in range(w["queries"]):
         gi = i % len(gs)
         queries.append((gi, grus.ALGO_SSSP, draw_source(rng, offs[gi])))
-    b = grus.Batch(gs)
+    # the project's autotuner chooses the engine's knobs for this mix (cached
+    # by graph set and mix; tuned here, outside the timed region, when new)
+    tuning = {"source": "library defaults (--no-tune)"}
+    bkw = {}
+    if not args.no_tune:
+        from grus_framework_gb300 import tuning_cache
+        tc = tuning_cache.load_or_tune_batch(gs, queries)
+        bkw = tc["config"]
+        tuning = {"source": "cache" if tc["cached"] else "grus_batch_autotune, this run",
+                  "config": bkw, "tuned_device_ms": round(tc["device_ms"], 3)}
+    b = grus.Batch(gs, **bkw)
     layout, total = b.layout(queries)
     out = torch.empty(total, dtype=torch.int32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -706,7 +716,7 @@ def run_batch(args, dist, rank, local):
                "queries": nq, "sources": "degree > 0, seed 4", "sum_n": int(sum(g.n for g in gs)),
                "sum_m": int(sum(g.m for g in gs)), "workers": info["workers"],
                "cluster_size": info["cluster_size"], "big_edges": info["big_edges"],
-               "launch_entries": info["launch_entries"],
+               "launch_entries": info["launch_entries"], "tuning": tuning,
                "l2": "flushed (256 MB write) before each step", "parallelism": f"replicas x{dist.get_world_size() if dist else 1}"}
         result = {
             "metric": w["metric"], "value": round(value, 1), "unit": QPS,
@@ -801,7 +811,24 @@ def run_serve(args, dist, rank, local):
     plain_qps = len(plain) / (time.perf_counter() - t0)
 
     qo = [[torch.empty(g.n, dtype=torch.int32, device="cuda") for _ in range(16)] for g in gs]
-    srv = grus.Server(gs)
+    # the server's knobs from the project's autotuner: saturated bursts of a
+    # mix drawn like the stream's (its own seed), cached by graph set and mix
+    tuning = {"source": "library defaults (--no-tune)"}
+    skw = {}
+    if not args.no_tune:
+        from grus_framework_gb300 import tuning_cache
+        trng = np.random.default_rng(w["seed"] + 1000)
+        tq = []
+        for _ in range(600):
+            gi = int(trng.integers(len(gs)))
+            tq.append((gi, grus.ALGO_SSSP if trng.random() < frac else grus.ALGO_BFS,
+                       draw_source(trng, offs[gi])))
+        tc = tuning_cache.load_or_tune_server(gs, tq)
+        skw = tc["config"]
+        tuning = {"source": "cache" if tc["cached"] else "grus_server_autotune, this run",
+                  "config": skw, "tuned_saturated_qps": round(tc["qps"], 1),
+                  "mix": "600 queries drawn like the stream (seed + 1000)"}
+    srv = grus.Server(gs, **skw)
     for _ in range(args.warmup):
         serve_stream(srv, grus, gs, qo, rng, offs, w["rate"], 200, frac)
     torch.cuda.synchronize()
@@ -888,8 +915,7 @@ def run_serve(args, dist, rank, local):
         cfg = {"workload": w["workload"], "graphs": "RMAT scales 16-22 and 24, edge factor 16, "
                                                      "seeds 50+scale, symmetrised, w in [1,255]",
                "offered_per_s": w["rate"], "queries": int(completed), "sssp_fraction": frac,
-               "sources": "degree > 0, seed 5", "server": "16 slots of 8-CTA workers, whole-GPU "
-               "lane for graphs of 2^20+ edges",
+               "sources": "degree > 0, seed 5", "tuning": tuning,
                "big_launches": int(st1["big_launches"] - st0["big_launches"]),
                "big_queries": int(st1["big_queries"] - st0["big_queries"]), "errors": int(errors),
                "parallelism": f"replicas x{dist.get_world_size() if dist else 1}"}
@@ -1044,6 +1070,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--scale", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="batched/served workloads: library defaults instead of the autotuner's")
     ap.add_argument("--no-systems", action="store_true",
                     help="default workload only: skip the batched and served summaries")
     args = ap.parse_args()

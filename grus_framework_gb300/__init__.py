@@ -86,7 +86,7 @@ class BatchConfig(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_uint32), ("cluster_size", C.c_uint32),
                 ("hbm_reserve_bytes", C.c_uint64), ("sssp_delta", C.c_uint32),
-                ("big_edges", C.c_uint32)]
+                ("big_edges", C.c_uint32), ("bfs_pack_min", C.c_uint32)]
 
 
 class Completion(C.Structure):
@@ -165,6 +165,10 @@ def _load():
         "grus_server_destroy": ([vp], i32),
         "grus_autotune": ([vp, u32, u32, i32, C.POINTER(Tuning), C.POINTER(C.c_float)], i32),
         "grus_cc": ([vp, vp, C.POINTER(Stats), vp], i32),
+        "grus_batch_autotune": ([C.POINTER(vp), i32, C.POINTER(Query), i32, i32,
+                                 C.POINTER(BatchConfig), C.POINTER(C.c_float)], i32),
+        "grus_server_autotune": ([C.POINTER(vp), i32, C.POINTER(Query), i32, i32,
+                                  C.POINTER(ServerConfig), C.POINTER(C.c_float)], i32),
         "grus_pagerank": ([vp, C.c_float, i32, vp, C.POINTER(Stats), vp], i32),
     }
     for name, (args, res) in sig.items():
@@ -603,9 +607,10 @@ class Server:
     """Query server over resident graphs (include/grus.h grus_server_*)."""
 
     def __init__(self, graphs, slots=16, cluster_size=8, hbm_reserve_bytes=0, sssp_delta=0,
-                 big_edges=0):
+                 big_edges=0, bfs_pack_min=0):
         self.graphs = list(graphs)
-        cfg = ServerConfig(slots, cluster_size, hbm_reserve_bytes, sssp_delta, big_edges)
+        cfg = ServerConfig(slots, cluster_size, hbm_reserve_bytes, sssp_delta, big_edges,
+                           bfs_pack_min)
         h = C.c_void_p()
         _check(lib.grus_server_create(_graph_array(self.graphs), len(self.graphs), C.byref(cfg),
                                       C.byref(h)), "grus_server_create")
@@ -637,6 +642,38 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def _query_array(graphs, queries):
+    arr = (Query * len(queries))()
+    at = 0
+    for i, (gi, algo, src) in enumerate(queries):
+        arr[i] = Query(gi, algo, src, 0, at)
+        at += graphs[gi].n
+    return arr
+
+
+def batch_autotune(graphs, queries, reps=2, start=None):
+    """Tunes the batch engine's knobs on this query mix (include/grus.h
+    grus_batch_autotune); returns (Batch keyword arguments, best device ms)."""
+    cfg = BatchConfig(**(start or {}))
+    ms = C.c_float()
+    _check(lib.grus_batch_autotune(_graph_array(graphs), len(graphs), _query_array(graphs, queries),
+                                   len(queries), reps, C.byref(cfg), C.byref(ms)),
+           "grus_batch_autotune")
+    return {k: getattr(cfg, k) for k, _ in cfg._fields_}, ms.value
+
+
+def server_autotune(graphs, queries, reps=1, start=None):
+    """Tunes the server's knobs for saturated throughput on this query mix
+    (include/grus.h grus_server_autotune); returns (Server keyword arguments,
+    best queries/s)."""
+    cfg = ServerConfig(**(start or {}))
+    qps = C.c_float()
+    _check(lib.grus_server_autotune(_graph_array(graphs), len(graphs), _query_array(graphs, queries),
+                                    len(queries), reps, C.byref(cfg), C.byref(qps)),
+           "grus_server_autotune")
+    return {k: getattr(cfg, k) for k, _ in cfg._fields_}, qps.value
 
 
 def autotune(g: Graph, algo=ALGO_BFS, src=None, reps=2):

@@ -72,6 +72,7 @@ struct grus_server {
   grus::GraphDesc *d_graphs = nullptr;
   uint64_t max_n = 0, max_m = 0;  // over the small graphs
   uint64_t big_edges = 1ull << 20;
+  uint32_t bfs_pack_min = 0;  // 0: grus::bfs_pack_min(m)
   int cluster = 8;
   uint32_t huge = 1024, delta = 192;
   uint64_t reserve = 1ull << 30;
@@ -378,7 +379,9 @@ void big_scheduler(grus_server *s) {
           size_t same = 1;
           for (const Request &q : s->big_pending)
             if (q.graph == first.graph && q.algo == GRUS_ALGO_BFS && ++same >= 64) break;
-          cap = same >= bfs_pack_min(s->graphs[first.graph]->m) ? 64 : 1;
+          const uint32_t pmin =
+              s->bfs_pack_min ? s->bfs_pack_min : bfs_pack_min(s->graphs[first.graph]->m);
+          cap = same >= pmin ? 64 : 1;
         }
         for (auto it = s->big_pending.begin(); it != s->big_pending.end() && j.group.size() < cap;) {
           if (it->graph == first.graph && it->algo == first.algo) {
@@ -433,6 +436,7 @@ int grus_server_create(grus_graph *const *graphs, int ngraphs, const grus_server
     if (cfg->hbm_reserve_bytes) s->reserve = cfg->hbm_reserve_bytes;
     if (cfg->sssp_delta) s->delta = cfg->sssp_delta;
     if (cfg->big_edges) s->big_edges = cfg->big_edges == 0xFFFFFFFFu ? ~0ull : cfg->big_edges;
+    s->bfs_pack_min = cfg->bfs_pack_min;
   }
   bool any_small = false;
   for (int i = 0; i < ngraphs; ++i) {

@@ -393,6 +393,10 @@ typedef struct grus_server_config {
   uint32_t sssp_delta;
   uint32_t big_edges;        /* graphs with at least this many edges run on the
                                 whole-GPU lane (default 2^20; 0xFFFFFFFF: never) */
+  uint32_t bfs_pack_min;     /* whole-GPU lane: fewest queued BFS requests on one
+                                graph that share one multi-source launch (up to
+                                64); 0 = by graph size (8 below 2^25 edges, 16
+                                below 2^27, 24 below 2^28, else 32) */
 } grus_server_config;
 
 typedef struct grus_completion {
@@ -422,6 +426,30 @@ GRUS_API int grus_server_submit(grus_server *s, uint32_t graph, uint32_t algo, u
 GRUS_API int grus_server_poll(grus_server *s, grus_completion *out, int max, int wait_ms);
 GRUS_API int grus_server_get_stats(grus_server *s, grus_server_stats *st);
 GRUS_API int grus_server_destroy(grus_server *s);
+
+/* ---- autotuning of the batched and served forms ------------------------------ */
+/* No counterpart in the reference, whose thresholds are fixed constants
+ * (include/common.cuh:30, include/frontier.cuh:140).  Both run coordinate
+ * descent over their engine's knobs on the caller's own query mix, starting
+ * from *best (zeros: defaults), and write the fastest setting back to *best.
+ * Results are the same under every setting, so tuning never trades
+ * correctness.  The graphs must stay unchanged while tuning runs.
+ *
+ * grus_batch_autotune: big_edges, launch_entries, cluster_size,
+ * group_sources and sssp_delta, each candidate timed as grus_batch_run with
+ * CUDA-graph replay (best of `reps` device times, *best_ms).  The query
+ * offsets define the output layout; the tuner allocates its own output. */
+GRUS_API int grus_batch_autotune(grus_graph *const *graphs, int ngraphs,
+                                 const grus_query *queries, int nq, int reps,
+                                 grus_batch_config *best, float *best_ms);
+/* grus_server_autotune: big_edges, bfs_pack_min, slots and cluster_size,
+ * each candidate a fresh server given every query at once (saturated
+ * throughput, host clock, best of `reps` bursts after a warm-up burst,
+ * *best_qps).  out_offset of the queries is ignored; a setting under which
+ * admission refuses queries is skipped. */
+GRUS_API int grus_server_autotune(grus_graph *const *graphs, int ngraphs,
+                                  const grus_query *queries, int nq, int reps,
+                                  grus_server_config *best, float *best_qps);
 
 #ifdef __cplusplus
 }

@@ -236,3 +236,56 @@ def test_batch_multi_graph_launches_split_past_64_graphs(grus):
     b.free()
     for g in gs:
         g.free()
+
+
+def _serve_all(grus, graphs, queries, **cfg):
+    import time
+    torch = pytest.importorskip("torch")
+    srv = grus.Server(graphs, **cfg)
+    outs = [torch.full((graphs[gi].n,), -7, dtype=torch.int32, device="cuda") for gi, _, _ in queries]
+    for i, (gi, algo, src) in enumerate(queries):
+        srv.submit(gi, algo, src, outs[i], i)
+    done = {}
+    t0 = time.time()
+    while len(done) < len(queries) and time.time() - t0 < 120:
+        for tag, st, _ in srv.poll(256, wait_ms=50):
+            done[tag] = st
+    srv.close()
+    assert len(done) == len(queries) and all(v == 0 for v in done.values())
+    return [o.cpu().numpy().view(np.uint32) for o in outs]
+
+
+def test_batch_autotune_keeps_results(grus, graphs):
+    """The batch autotuner (grus_batch_autotune) picks the fastest engine
+    setting for a query mix; the tuned batch gives the same bits as the
+    default one and as single queries."""
+    torch = pytest.importorskip("torch")
+    queries = make_queries(grus, graphs, 48, 11)
+    cfg, ms = grus.batch_autotune(graphs, queries, reps=1)
+    assert ms > 0 and set(cfg) >= {"big_edges", "launch_entries", "cluster_size"}
+    outs = []
+    for kw in ({}, cfg):
+        b = grus.Batch(graphs, **kw)
+        offs, total = b.layout(queries)
+        out = torch.full((total,), -7, dtype=torch.int32, device="cuda")
+        b.run(queries, out, offs, use_graph=True)
+        outs.append(out.cpu().numpy().view(np.uint32))
+        b.free()
+    assert np.array_equal(outs[0], outs[1])
+    for q, o in zip(queries, offs):
+        ref = reference(grus, graphs, q)
+        assert np.array_equal(outs[1][o:o + len(ref)], ref), q
+
+
+def test_server_autotune_keeps_results(grus, graphs):
+    """The server autotuner (grus_server_autotune) times saturated bursts of
+    the mix under each setting; a server built with the result, and one with
+    BFS packs forced from two queued requests, serve the same bits as single
+    queries."""
+    queries = make_queries(grus, graphs, 64, 12)
+    cfg, qps = grus.server_autotune(graphs, queries, reps=1)
+    assert qps > 0 and "bfs_pack_min" in cfg
+    for kw in (cfg, dict(big_edges=1, bfs_pack_min=2)):
+        got = _serve_all(grus, graphs, queries, **kw)
+        for q, o in zip(queries, got):
+            assert np.array_equal(o, reference(grus, graphs, q)), (kw, q)

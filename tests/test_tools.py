@@ -86,3 +86,16 @@ def test_telemetry_without_device(grus_lib):
     with pytest.raises(grus_lib.GrusError) as e:
         grus_lib.telemetry()
     assert e.value.status == grus_lib.ENODEV
+
+
+def test_tuning_cache_mix_signature():
+    """Batch/server tunings are keyed by graph set and query mix: the key
+    changes when either changes and is stable otherwise."""
+    from grus_framework_gb300 import tuning_cache as tc
+    gs = ["0:100:400:3:7:12", "0:50:90:3:1:9"]
+    q = [(0, 1, 5), (1, 0, 7)]
+    k = tc.mix_signature("batch", gs, q)
+    assert k == tc.mix_signature("batch", list(gs), [tuple(x) for x in q])
+    assert k != tc.mix_signature("server", gs, q)
+    assert k != tc.mix_signature("batch", gs[::-1], q)
+    assert k != tc.mix_signature("batch", gs, [(0, 1, 6), (1, 0, 7)])
