@@ -32,6 +32,22 @@ def load(path: Path = DEFAULT_PATH) -> dict:
         return {}
 
 
+def _store(path: Path, key: str, entry: dict) -> bool:
+    """Adds one entry to the cache file; an unwritable cache only costs the
+    reuse (returns False), never the tuning just measured."""
+    cache = load(path)
+    cache[key] = entry
+    path = Path(path)
+    try:
+        path.parent.mkdir(parents=True, exist_ok=True)
+        tmp = path.with_suffix(".tmp")
+        tmp.write_text(json.dumps(cache, indent=1))
+        tmp.replace(path)
+    except OSError:
+        return False
+    return True
+
+
 def load_or_tune(g: "grus.Graph", algo: int = grus.ALGO_BFS, src=None, path: Path = DEFAULT_PATH,
                  reps: int = 2) -> dict:
     """Applies the cached tuning for `g`, or autotunes and caches it."""
@@ -41,23 +57,9 @@ def load_or_tune(g: "grus.Graph", algo: int = grus.ALGO_BFS, src=None, path: Pat
         g.set_tuning(**cache[key]["tuning"])
         return cache[key]
     tuning, ms = grus.autotune(g, algo, src, reps)
-    cache[key] = {"tuning": tuning, "device_ms": ms}
-    path = Path(path)
-    path.parent.mkdir(parents=True, exist_ok=True)
-    tmp = path.with_suffix(".tmp")
-    tmp.write_text(json.dumps(cache, indent=1))
-    tmp.replace(path)
-    return cache[key]
-
-
-def _store(path: Path, key: str, entry: dict) -> None:
-    cache = load(path)
-    cache[key] = entry
-    path = Path(path)
-    path.parent.mkdir(parents=True, exist_ok=True)
-    tmp = path.with_suffix(".tmp")
-    tmp.write_text(json.dumps(cache, indent=1))
-    tmp.replace(path)
+    entry = {"tuning": tuning, "device_ms": ms}
+    _store(path, key, entry)
+    return entry
 
 
 def mix_signature(kind: str, graph_sigs, queries) -> str:

@@ -99,3 +99,15 @@ def test_tuning_cache_mix_signature():
     assert k != tc.mix_signature("server", gs, q)
     assert k != tc.mix_signature("batch", gs[::-1], q)
     assert k != tc.mix_signature("batch", gs, [(0, 1, 6), (1, 0, 7)])
+
+
+def test_tuning_cache_unwritable_location(tmp_path):
+    """A cache that cannot be written only loses the reuse: the store reports
+    it and nothing is raised; a writable one round-trips."""
+    from grus_framework_gb300 import tuning_cache as tc
+    blocked = tmp_path / "file"
+    blocked.write_text("not a directory")
+    assert tc._store(blocked / "sub" / "t.json", "k", {"x": 1}) is False
+    ok = tmp_path / "cache" / "t.json"
+    assert tc._store(ok, "k", {"x": 1}) is True
+    assert tc.load(ok) == {"k": {"x": 1}}
