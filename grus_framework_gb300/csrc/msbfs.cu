@@ -49,6 +49,7 @@ struct Slot {
   uint32_t pad;
   unsigned long long mf;  // out-edges of the frontier
   unsigned long long bits;
+  unsigned long long live;  // sources present in the level's frontier words
 };
 
 struct Summary {
@@ -199,6 +200,7 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
       }
       const uint32_t t = atomicAdd(&a.slots[0].tcount, 1u);
       a.touched[0][t] = s;
+      atomicOr(&a.slots[0].live, a.full);
       const uint32_t b = __ldg(a.offs + s), e = __ldg(a.offs + s + 1);
       atomicAdd(&a.slots[0].mf, (unsigned long long)(e - b));
       if (!push_binned(s, b, e, a.huge, a.queue[0], &a.slots[0].qcount, a.cap, a.chunks[0],
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
     uint4 *cnext = a.chunks[(L + 1) & 1u];
     if (gtid < sizeof(Slot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[gtid] = 0u;
     const uint32_t val = L + 1;
-    unsigned long long mf = 0, nbits = 0;
+    unsigned long long mf = 0, nbits = 0, live = 0;
     if (!pull) {
       // phase A: push -- accumulate new bits of every touched vertex
       PushVisitor vis{&a, fcur, acc, tnext, &nx->tcount};
@@ -240,6 +242,7 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
           const uint32_t b = __ldg(a.offs + u), e = __ldg(a.offs + u + 1);
           mf += e - b;
           nbits += __popcll(bits);
+          live |= bits;
           if (!push_binned(u, b, e, a.huge, qnext, &nx->qcount, a.cap, cnext, &nx->ccount,
                            a.chunk_cap))
             atomicOr(a.err, kErrOverflow);
@@ -247,20 +250,27 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
       }
     } else {
       // phase A: pull -- every vertex missing bits ORs its in-neighbours'
-      // frontier words.  A lane scans the first kPullLane in-edges of its
+      // frontier words.  Only sources present in those words can add a bit
+      // (a source whose frontier died -- one outside the vertex's component
+      // -- never will), so a vertex looks for the live sources it misses and
+      // is skipped when it misses none.  A lane scans the first kPullLane in-edges of its
       // vertex (four gathers in flight) and stops once no bit is missing;
       // longer lists still missing bits are finished by the whole warp, one
       // vertex at a time, 32 edges per step, so a high-degree vertex costs
       // its warp deg/32 steps instead of deg serial loads on one lane.
       ++pull_levels;
+      const unsigned long long lv = __ldcg(&cur->live);
       const uint32_t gw = gtid >> 5, nw = nthreads >> 5;
       for (uint32_t w = gw; w * 32 < a.n; w += nw) {
         const uint32_t u = w * 32 + lane;
         unsigned long long bits = 0, vis = a.full, accb = 0;
+        // `want`: vis plus every source that cannot add a bit at this level
+        unsigned long long want = a.full;
         uint32_t rest_b = 0, rest_e = 0;
         if (u < a.n) {
           vis = __ldcg(a.visit + u);
-          if (vis != a.full) {
+          want = vis | (a.full & ~lv);
+          if (want != a.full) {
             const uint32_t b = __ldg(a.ioffs + u), e = __ldg(a.ioffs + u + 1);
             const uint32_t lim = min(e, b + kPullLane);
             uint32_t x = b;
@@ -268,11 +278,11 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
               const uint32_t c0 = __ldg(a.icols + x), c1 = __ldg(a.icols + x + 1);
               const uint32_t c2 = __ldg(a.icols + x + 2), c3 = __ldg(a.icols + x + 3);
               accb |= __ldcg(fcur + c0) | __ldcg(fcur + c1) | __ldcg(fcur + c2) | __ldcg(fcur + c3);
-              if ((accb | vis) == a.full) break;
+              if ((accb | want) == a.full) break;
             }
-            if ((accb | vis) != a.full) {
+            if ((accb | want) != a.full) {
               for (; x < lim; ++x) accb |= __ldcg(fcur + __ldg(a.icols + x));
-              if ((accb | vis) != a.full && e > lim) {
+              if ((accb | want) != a.full && e > lim) {
                 rest_b = lim;
                 rest_e = e;
               }
@@ -286,7 +296,7 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
           const uint32_t rb = __shfl_sync(0xffffffffu, rest_b, sl);
           const uint32_t re = __shfl_sync(0xffffffffu, rest_e, sl);
           const unsigned long long have =
-              __shfl_sync(0xffffffffu, accb | vis, sl);
+              __shfl_sync(0xffffffffu, accb | want, sl);
           unsigned long long wacc = 0;
           for (uint32_t base = rb; base < re; base += 32) {
             const uint32_t x = base + lane;
@@ -296,7 +306,7 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
           wacc = warp_or64(wacc);
           if (lane == sl) accb |= wacc;
         }
-        if (u < a.n && vis != a.full) {
+        if (u < a.n && want != a.full) {
           bits = accb & ~vis;
           if (bits) {
             acc[u] = bits;
@@ -304,6 +314,7 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
             const uint32_t ob = __ldg(a.offs + u), oe = __ldg(a.offs + u + 1);
             mf += oe - ob;
             nbits += __popcll(bits);
+            live |= bits;
             const uint32_t pos = agg_reserve(&nx->tcount);
             if (pos < a.cap) tnext[pos] = u;
             if (!push_binned(u, ob, oe, a.huge, qnext, &nx->qcount, a.cap, cnext, &nx->ccount,
@@ -325,6 +336,9 @@ __global__ void __launch_bounds__(kBlock, 8) msbfs_persistent(Args a) {
     for (uint32_t i = gtid; i < tcc; i += nthreads) fcur[__ldcg(tcur + i)] = 0ull;
     const unsigned long long bmf = block_sum_u64<kBlock>(mf);
     const unsigned long long bnb = block_sum_u64<kBlock>(nbits);
+    // OR of the bits that entered the next frontier: one reduction per warp
+    for (int o = 16; o > 0; o >>= 1) live |= __shfl_xor_sync(0xffffffffu, live, o);
+    if (lane == 0 && live) atomicOr(&nx->live, live);
     if (threadIdx.x == 0 && (bmf || bnb)) {
       atomicAdd(&nx->mf, bmf);
       atomicAdd(&nx->bits, bnb);

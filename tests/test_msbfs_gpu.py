@@ -94,3 +94,22 @@ def test_msbfs_rejects_bad_arguments(grus):
         grus.bfs_multi(g, np.zeros(65, np.uint32))
     with pytest.raises(grus.GrusError):
         grus.bfs_multi(g, np.array([g.n], np.uint32))
+
+
+def test_msbfs_source_outside_the_giant_component(grus, oracle_mod):
+    """A source in a small component stops expanding after a few levels; the
+    pull levels must stop looking for its bit elsewhere (they search only the
+    sources present in the frontier) and every row stays exact."""
+    g = grus.Graph.rmat(14, 16, 4, symmetric=True)
+    h = host_csr(g)
+    deg = np.diff(h.offs.astype(np.int64))
+    d = oracle_mod.bfs(h, g.max_degree_vertex)
+    small = np.flatnonzero((deg > 0) & (d == INF))
+    giant = np.flatnonzero(d != INF)
+    assert len(small) > 0
+    srcs = np.concatenate([small[:2], giant[::max(1, len(giant) // 40)][:40]]).astype(np.uint32)
+    for alpha in (0.0, 1e-3):  # default switch, and pull from the first level on
+        if alpha:
+            g.set_tuning(multi_alpha=alpha)
+        st = check(grus, oracle_mod, g, srcs)
+    assert st["bottom_up_levels"] >= 1
