@@ -108,8 +108,7 @@ def test_msbfs_source_outside_the_giant_component(grus, oracle_mod):
     giant = np.flatnonzero(d != INF)
     assert len(small) > 0
     srcs = np.concatenate([small[:2], giant[::max(1, len(giant) // 40)][:40]]).astype(np.uint32)
-    for alpha in (0.0, 1e-3):  # default switch, and pull from the first level on
-        if alpha:
-            g.set_tuning(multi_alpha=alpha)
-        st = check(grus, oracle_mod, g, srcs)
-    assert st["bottom_up_levels"] >= 1
+    check(grus, oracle_mod, g, srcs)  # the default switch
+    g.set_tuning(multi_alpha=1e9)     # pull from the second level on
+    st = check(grus, oracle_mod, g, srcs)
+    assert st["bottom_up_levels"] >= 2
