@@ -99,15 +99,17 @@ def test_msbfs_rejects_bad_arguments(grus):
 def test_msbfs_source_outside_the_giant_component(grus, oracle_mod):
     """A source in a small component stops expanding after a few levels; the
     pull levels must stop looking for its bit elsewhere (they search only the
-    sources present in the frontier) and every row stays exact."""
-    g = grus.Graph.rmat(14, 16, 4, symmetric=True)
-    h = host_csr(g)
-    deg = np.diff(h.offs.astype(np.int64))
-    d = oracle_mod.bfs(h, g.max_degree_vertex)
-    small = np.flatnonzero((deg > 0) & (d == INF))
-    giant = np.flatnonzero(d != INF)
-    assert len(small) > 0
-    srcs = np.concatenate([small[:2], giant[::max(1, len(giant) // 40)][:40]]).astype(np.uint32)
+    sources present in the frontier) and every row stays exact.  The graph is
+    RMAT-14 with a three-vertex path appended as a component of its own."""
+    base = host_csr(grus.Graph.rmat(14, 16, 4, symmetric=True))
+    n = base.n
+    offs = np.concatenate([base.offs, base.offs[-1] + np.array([1, 3, 4], np.uint32)]).astype(np.uint32)
+    cols = np.concatenate([base.cols[:base.m], np.array([n + 1, n, n + 2, n + 1], np.uint32)])
+    g = grus.Graph.from_csr(offs, cols, symmetric=True)
+    deg = np.diff(offs.astype(np.int64))
+    giant = np.flatnonzero(oracle_mod.bfs(host_csr(g), g.max_degree_vertex) != INF)
+    srcs = np.concatenate([[n, n + 2], giant[::max(1, len(giant) // 40)][:40]]).astype(np.uint32)
+    assert deg[n] > 0 and deg[n + 2] > 0
     check(grus, oracle_mod, g, srcs)  # the default switch
     g.set_tuning(multi_alpha=1e9)     # pull from the second level on
     st = check(grus, oracle_mod, g, srcs)
