@@ -432,6 +432,13 @@ def run_grus(args, dist, rank, local):
             return grus.sssp_multi(g, srcs, out=out, stream=stream, stats=stats)
         return grus.bfs_multi(g, srcs, out=out, stream=stream, stats=stats)
 
+    # BFS: the per-graph pull index (4 bytes per vertex) is built before the
+    # first call, like the graph itself; its build time goes into the line
+    index = None
+    if algo == "bfs" and (w.get("symmetric", True) or w["graph"] == "grid"):
+        index = {"bytes": 4 * n, "build_ms": round(g.build_index(), 3),
+                 "what": "per vertex, an in-neighbour of high out-degree, tested before the "
+                         "vertex's adjacency in pull levels"}
     out_dev = make_out(False)
     _, st = call(out_dev, stats=True)
     nr, mr = st["vertices_reached"], st["edges_reached"]
@@ -538,6 +545,8 @@ def run_grus(args, dist, rank, local):
                     "parallelism": f"replicas x{ws}", "levels": st["levels"],
                     "bottom_up_levels": st["bottom_up_levels"],
                     "vertices_reached": nr, "edges_reached": mr})
+        if index:
+            cfg["bfs_pull_index"] = index
         result = {
             "metric": w["metric"], "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(mean_ms, 4),

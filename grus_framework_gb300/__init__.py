@@ -144,6 +144,7 @@ def _load():
         "grus_graph_get_info": ([vp, C.POINTER(GraphInfo)], i32),
         "grus_graph_copy_csr": ([vp, vp, vp, vp], i32),
         "grus_graph_build_csc": ([vp], i32),
+        "grus_graph_build_index": ([vp, C.POINTER(C.c_float)], i32),
         "grus_graph_copy_csc": ([vp, vp, vp, vp], i32),
         "grus_graph_set_tuning": ([vp, C.POINTER(Tuning)], i32),
         "grus_graph_get_tuning": ([vp, C.POINTER(Tuning)], i32),
@@ -396,6 +397,13 @@ class Graph:
 
     def build_csc(self):
         _check(lib.grus_graph_build_csc(self._handle()), "grus_graph_build_csc")
+
+    def build_index(self) -> float:
+        """Builds the BFS pull index now (include/grus.h
+        grus_graph_build_index); returns its build time in device ms."""
+        ms = C.c_float()
+        _check(lib.grus_graph_build_index(self._handle(), C.byref(ms)), "grus_graph_build_index")
+        return ms.value
 
     def copy_csc(self):
         inf = self.info()

@@ -113,6 +113,7 @@ struct Args {
   const uint32_t *__restrict__ cols;
   const uint32_t *__restrict__ ioffs;  // in-edges (pull levels): the CSR itself
   const uint32_t *__restrict__ icols;  // on a symmetric graph, else the CSC
+  const uint32_t *__restrict__ rep;    // pull index (null: none), grus_graph::bfs_rep
   bool allow_pull;                     // false when no in-edge arrays exist
   uint32_t n, W;
   uint64_t m;
@@ -299,6 +300,16 @@ __device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32
         lim[k] = min(e[k], b[k] + scan);
       }
     }
+    // the representative in-neighbour first (coalesced); only vertices it
+    // does not settle read their adjacency below
+    if (a.rep) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const uint32_t v = (w0 + k) * 32 + lane;
+        const uint32_t r = act[k] ? __ldg(a.rep + v) : kNoRep;
+        found[k] = r != kNoRep && test_bit(fcur, r);
+      }
+    }
     // probe rounds: four neighbours per word, K words at once
     for (uint32_t r = 0; r < scan; r += 4) {
       uint32_t u[K][4];
@@ -389,11 +400,14 @@ __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, co
     for (int k = 0; k < K; ++k) {
       found[k] = false;
       b[k] = e[k] = lim[k] = 0;
+      uint32_t r = kNoRep;
       if (act[k]) {
         b[k] = __ldg(a.ioffs + v[k]);
         e[k] = __ldg(a.ioffs + v[k] + 1);
         lim[k] = min(e[k], b[k] + scan);
+        if (a.rep) r = __ldg(a.rep + v[k]);
       }
+      found[k] = r != kNoRep && test_bit(fcur, r);
     }
     for (uint32_t r = 0; r < scan; r += 4) {
       uint32_t u[K][4];
@@ -1009,6 +1023,11 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
     a.icols = g->csr.cols;
   }
   a.allow_pull = a.ioffs != nullptr;
+  if (a.allow_pull) {
+    rc = build_rep_locked(g);
+    if (rc) return rc;
+    a.rep = g->bfs_rep;
+  }
   a.n = (uint32_t)g->n;
   a.W = w->W;
   a.m = g->m;

@@ -340,6 +340,69 @@ int graph_from_host(uint64_t n, uint64_t m, const uint32_t *offs,
   return GRUS_OK;
 }
 
+// rep[v]: among the first kRepScan in-neighbours of v, one of largest
+// out-degree (the first such), or kNoRep.  One warp per vertex; the key
+// (out-degree, -position) is reduced across the lanes.  A BFS pull level tests
+// this vertex's frontier bit before reading v's adjacency: high-degree
+// neighbours are reached early, so for nearly every vertex found at a pull
+// level (99.4-100 % on RMAT-20) the representative is already in the
+// frontier and the scattered read of the list is skipped.  Any in-neighbour
+// would keep results exact; the bound keeps the build at one pass.
+constexpr uint32_t kRepScan = 256;
+__global__ void k_build_rep(const uint32_t *__restrict__ ioffs, const uint32_t *__restrict__ icols,
+                            const uint32_t *__restrict__ offs, uint32_t n, uint32_t *rep) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nw) {
+    const uint32_t b = ioffs[v], e = min(ioffs[v + 1], b + kRepScan);
+    unsigned long long best = 0;
+    for (uint32_t x = b + lane; x < e; x += 32) {
+      const uint32_t u = icols[x];
+      const unsigned long long key =
+          ((unsigned long long)(offs[u + 1] - offs[u] + 1u) << 32) | (0xFFFFFFFFu - (x - b));
+      best = key > best ? key : best;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_xor_sync(0xffffffffu, best, o);
+      best = t > best ? t : best;
+    }
+    if (lane == 0) rep[v] = best ? icols[b + (0xFFFFFFFFu - (uint32_t)best)] : kNoRep;
+  }
+}
+
+int build_rep_locked(grus_graph *g) {
+  if (g->bfs_rep) return GRUS_OK;
+  const bool sym = (g->flags & GRUS_GRAPH_SYMMETRIC) != 0;
+  const uint32_t *io = sym ? g->csr.offs : g->csc.offs;
+  const uint32_t *ic = sym ? g->csr.cols : g->csc.cols;
+  if (!io) return GRUS_EINVAL;
+  uint32_t *rep = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMalloc(&rep, std::max<uint64_t>(g->n, 1) * 4);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) {
+    cudaEventRecord(e0, 0);
+    const int sms = std::max(device_sm_count(), 1);
+    if (g->n) k_build_rep<<<sms * 8, 256>>>(io, ic, g->csr.offs, (uint32_t)g->n, rep);
+    cudaEventRecord(e1, 0);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) {
+    if (rep) cudaFree(rep);
+    set_last_error(std::string("bfs pull index: ") + cudaGetErrorString(e));
+    return status_from_cuda(e);
+  }
+  g->bfs_rep = rep;
+  g->bfs_rep_ms = ms;
+  return GRUS_OK;
+}
+
 // Device transpose: stable radix sort of column ids carrying edge ids, so each
 // CSC column lists its rows in ascending order exactly as the counting sort of
 // include/graph.cuh:273-303 does; weights are permuted along (the reference
@@ -713,6 +776,19 @@ int grus_graph_build_csc(grus_graph *g) {
   return build_csc_locked(g);
 }
 
+int grus_graph_build_index(grus_graph *g, float *build_ms) {
+  if (!g) return GRUS_EINVAL;
+  std::lock_guard<std::mutex> lk(g->mu);
+  if (!(g->flags & GRUS_GRAPH_SYMMETRIC)) {
+    const int rc = build_csc_locked(g);
+    if (rc) return rc;
+  }
+  const int rc = build_rep_locked(g);
+  if (rc) return rc;
+  if (build_ms) *build_ms = g->bfs_rep_ms;
+  return GRUS_OK;
+}
+
 int grus_graph_set_tuning(grus_graph *g, const grus_tuning *t) {
   if (!g || !t) return GRUS_EINVAL;
   if (t->alpha < 0.f || t->beta < 0.f || t->multi_alpha < 0.f || t->ctas_per_sm > 64)
@@ -750,6 +826,7 @@ int grus_graph_free(grus_graph *g) {
   if (g->csr.offs) cudaFree(g->csr.offs);
   if (g->csr.cols) cudaFree(g->csr.cols);
   if (g->csr.wts) cudaFree(g->csr.wts);
+  if (g->bfs_rep) cudaFree(g->bfs_rep);
   if (g->balloon) cudaFree(g->balloon);
   delete g;
   return GRUS_OK;

@@ -54,6 +54,10 @@ struct grus_graph {
   grus::Csr csr;              // out-edges
   grus::Csr csc;              // in-edges (built on demand; aliases csr if symmetric)
   uint32_t max_deg_vertex = 0, max_deg = 0;
+  // BFS pull index: per vertex, an in-neighbour of high out-degree (built on
+  // demand, grus::build_rep_locked), kNoRep without in-edges
+  uint32_t *bfs_rep = nullptr;
+  float bfs_rep_ms = 0.f;
   grus_tuning tuning{};       // zero fields = library defaults
   std::mutex mu;              // guards the workspaces and the csc build
   void *ws[grus::kWsCount] = {};
@@ -67,6 +71,10 @@ void graph_free_array(grus_graph *g, void *p);
 int device_sm_count();
 int l2_window(cudaStream_t s, void *base, size_t bytes);
 int build_csc_locked(grus_graph *g);
+// Builds g->bfs_rep for the graph's in-edges (the CSR of a symmetric graph,
+// else the CSC, which must exist); no-op when built.  Caller holds g->mu.
+constexpr uint32_t kNoRep = 0xFFFFFFFFu;
+int build_rep_locked(grus_graph *g);
 
 // Effective tuning value: the graph's setting when non-zero, else `def`.
 template <typename T>

@@ -201,3 +201,25 @@ def test_bfs_long_tail_with_sinks(grus, oracle_mod):
     offs[path + 1:] = offs[path]
     g = grus.Graph.from_csr(offs, np.array(cols, np.uint32))
     _check_bfs(grus, oracle_mod, g, [0, 7, path - 1, path + 3])
+
+
+def test_bfs_pull_index(grus, oracle_mod):
+    """The pull index (one representative in-neighbour per vertex) is built
+    once per graph, on demand or ahead of the first BFS, and BFS depths with
+    it are exact on symmetric and directed graphs."""
+    for sym in (True, False):
+        g = grus.Graph.rmat(14, 16, 11, symmetric=sym)
+        if not sym:
+            g.build_csc()
+        ms = g.build_index()
+        assert ms >= 0.0
+        assert g.build_index() == ms  # built once
+        offs, cols, _ = g.copy_csr()
+        h = oracle_mod.CSR(offs, cols)
+        deg = np.diff(offs.astype(np.int64))
+        for src in (g.max_degree_vertex, int(np.flatnonzero(deg > 0)[3])):
+            d, st = grus.bfs(g, src, stats=True)
+            assert np.array_equal(d, oracle_mod.bfs(h, src))
+        if sym:
+            assert st["bottom_up_levels"] >= 1
+        g.free()
