@@ -80,7 +80,8 @@ struct LevelSlot {
   uint32_t nf;             // vertices discovered into this level
   uint32_t scount;         // pull: vertices left unresolved, with in-edges
   unsigned long long mf;   // sum of their out-degrees
-  unsigned long long pad2;
+  uint32_t dcount;         // pull with the index: vertices it left to probe
+  uint32_t pad2;
 };
 
 struct Summary {
@@ -119,6 +120,13 @@ struct Args {
   uint64_t m;
   uint32_t src;
   uint32_t *depth;
+  // Depths as bit planes (null: depths are stored as vertices are found):
+  // bit p of vertex v's depth is bit v of plane p (planes[p * Wp + v / 32]).
+  // Setting bits in L2-resident words replaces scattered 4-byte stores into
+  // the depth array, each a partial write of a sector in HBM; the depth
+  // array is then written once, whole lines, when the traversal ends.
+  uint32_t *planes;
+  uint32_t Wp, nplanes;
   uint32_t *visited;      // W words; fronts follow contiguously
   uint32_t *front[3];
   uint32_t *queue[2];
@@ -140,8 +148,9 @@ struct Workspace {
   uint64_t n = 0, m = 0;
   uint32_t W = 0;
   uint32_t *depth = nullptr;     // used when the caller's buffer is on the host
-  uint32_t *bitmaps = nullptr;   // visited + 3 fronts, 4*Wp words
-  size_t bitmap_bytes = 0;
+  uint32_t *bitmaps = nullptr;   // visited + 3 fronts + depth planes, (4+P)*Wp words
+  size_t bitmap_bytes = 0;       // the part kept in the L2 persisting window
+  uint32_t nplanes = 0;          // P: bits of the largest possible depth
   uint32_t *queues = nullptr;    // 2 * n
   uint4 *chunks = nullptr;       // 2 * chunk_cap
   uint32_t chunk_cap = 0;
@@ -186,13 +195,18 @@ int ws_get(grus_graph *g, Workspace **out) {
   w->m = g->m;
   w->W = (uint32_t)((g->n + 31) / 32);
   const uint64_t Wp = ((uint64_t)w->W + 31) / 32 * 32;  // 128-byte aligned maps
-  w->bitmap_bytes = 4 * Wp * 4;
+  // depths reach at most n - 1; the window covers the maps and the planes of
+  // depths below 16
+  uint32_t P = 1;
+  while (P < 32 && (g->n >> P) != 0) ++P;
+  w->nplanes = P;
+  w->bitmap_bytes = (4 + std::min<uint64_t>(P, 4)) * Wp * 4;
   // chunk lists sized for any chunking degree down to 256 (the autotuner and
   // callers may lower it after the workspace exists)
   const uint32_t huge = std::min(tune_or(g->tuning.huge_degree, kDefHuge), 256u);
   const uint64_t cap = g->m / kChunk + g->m / std::max(huge, 1u) + 2;
   w->chunk_cap = (uint32_t)std::min<uint64_t>(cap, 0x7FFFFFFFull);
-  cudaError_t e = cudaMalloc(&w->bitmaps, w->bitmap_bytes);
+  cudaError_t e = cudaMalloc(&w->bitmaps, (4 + (uint64_t)P) * Wp * 4);
   if (e == cudaSuccess) e = cudaMalloc(&w->queues, 2 * std::max<uint64_t>(g->n, 1) * 4);
   if (e == cudaSuccess) e = cudaMalloc(&w->chunks, 2ull * w->chunk_cap * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
@@ -212,6 +226,45 @@ int ws_get(grus_graph *g, Workspace **out) {
   g->ws_free[kWsBfs] = ws_free;
   *out = w;
   return GRUS_OK;
+}
+
+// Records depth nd for the vertices of `mask` in word w: one non-returning
+// atomicOr per set bit of nd into the bit planes, else plain stores of nd.
+__device__ __forceinline__ void mark_depth(const Args &a, uint32_t w, uint32_t mask, uint32_t nd) {
+  uint32_t d = nd;
+  for (uint32_t p = 0; d; ++p, d >>= 1)
+    if (d & 1u) atomicOr(a.planes + (size_t)p * a.Wp + w, mask);
+}
+
+// Writes every vertex's depth from the bit planes of depths below 2^np and
+// the visited bitmap (unreached: INFINIT): a warp turns K words into K whole
+// 128-byte lines of the depth array per step.
+__device__ __noinline__ void write_depths(const Args &a, uint32_t np) {
+  constexpr int KM = 4;
+  const uint32_t lane = lane_id();
+  const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kBlock) >> 5;
+  for (uint32_t w0 = gw * KM; w0 < a.W; w0 += nw * KM) {
+    uint32_t vis[KM], d[KM];
+#pragma unroll
+    for (int k = 0; k < KM; ++k) {
+      vis[k] = w0 + k < a.W ? __ldcg(a.visited + w0 + k) : 0u;
+      d[k] = 0u;
+    }
+    for (uint32_t p = 0; p < np; ++p) {
+      const uint32_t *pl = a.planes + (size_t)p * a.Wp;
+#pragma unroll
+      for (int k = 0; k < KM; ++k) {
+        const uint32_t pw = w0 + k < a.W ? __ldcg(pl + w0 + k) : 0u;
+        d[k] |= ((pw >> lane) & 1u) << p;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < KM; ++k) {
+      const uint32_t v = (w0 + k) * 32 + lane;
+      if (w0 + k < a.W && v < a.n) a.depth[v] = ((vis[k] >> lane) & 1u) ? d[k] : kInfinit;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -236,7 +289,8 @@ struct PushVisitor {
     const uint32_t w = dst >> 5, bit = 1u << (dst & 31u);
     if (__ldcg(a->visited + w) & bit) return;
     if (atomicOr(a->visited + w, bit) & bit) return;
-    a->depth[dst] = nd;
+    if (a->planes) mark_depth(*a, w, bit, nd);
+    else a->depth[dst] = nd;
     atomicOr(fnext + w, bit);
     const uint32_t b = __ldg(a->offs + dst), e = __ldg(a->offs + dst + 1);
     nf += 1;
@@ -355,9 +409,10 @@ __device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32
         if (lane == 0) {
           a.visited[w] = vis[k] | mask;
           fnext[w] = mask;
+          if (a.planes) mark_depth(a, w, mask, nd);
         }
         if (found[k]) {
-          a.depth[v] = nd;
+          if (!a.planes) a.depth[v] = nd;
           nf += 1;
           mf += __ldg(a.offs + v + 1) - __ldg(a.offs + v);
         }
@@ -366,6 +421,57 @@ __device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32
       if (lane == 0 && w < a.W) {
         sbm[w] = smask;
         ns += __popc(smask);
+      }
+    }
+  }
+}
+
+// First pull level with the pull index: each unvisited vertex tests only its
+// representative in-neighbour (one coalesced load and one frontier bit), so a
+// warp step never waits on adjacency reads.  Vertices it leaves unresolved
+// that have in-edges are marked in `dbm` (one plain store per word by the
+// warp that owns it) and probed afterwards from a dense queue by
+// bu_level_survivors: with the probes of the few unresolved lanes removed
+// from the word pass, its steps no longer wait on the adjacency reads of one
+// or two lanes each.
+template <int K>
+__device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const uint32_t *fcur,
+                                             uint32_t *fnext, uint32_t &nf, unsigned long long &mf,
+                                             uint32_t *dbm) {
+  const uint32_t nd = L + 1;
+  const uint32_t lane = lane_id();
+  const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kBlock) >> 5;
+  for (uint32_t w0 = gw * K; w0 < a.W; w0 += nw * K) {
+    uint32_t vis[K], r[K], b[K], e[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) vis[k] = w0 + k < a.W ? __ldcg(a.visited + w0 + k) : 0xFFFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint32_t v = (w0 + k) * 32 + lane;
+      const bool act = !((vis[k] >> lane) & 1u) && v < a.n;
+      r[k] = act ? __ldg(a.rep + v) : kNoRep;
+      b[k] = act ? __ldg(a.offs + v) : 0u;
+      e[k] = act ? __ldg(a.offs + v + 1) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const bool found = r[k] != kNoRep && test_bit(fcur, r[k]);
+      const uint32_t mask = __ballot_sync(0xffffffffu, found);
+      const uint32_t dmask = __ballot_sync(0xffffffffu, r[k] != kNoRep && !found);
+      const uint32_t w = w0 + k, v = w * 32 + lane;
+      if (found) {
+        if (!a.planes) a.depth[v] = nd;
+        nf += 1;
+        mf += e[k] - b[k];
+      }
+      if (lane == 0 && w < a.W) {
+        if (mask) {
+          a.visited[w] = vis[k] | mask;
+          fnext[w] = mask;
+          if (a.planes) mark_depth(a, w, mask, nd);
+        }
+        dbm[w] = dmask;
       }
     }
   }
@@ -381,7 +487,8 @@ template <int K>
 __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, const uint32_t *fcur,
                                                    uint32_t *fnext, const uint32_t *sin,
                                                    uint32_t S, uint32_t &nf, unsigned long long &mf,
-                                                   uint32_t *sq, uint32_t *scount) {
+                                                   uint32_t *sq, uint32_t *scount,
+                                                   bool use_rep = true) {
   const uint32_t nd = L + 1;
   const uint32_t lane = lane_id();
   const uint32_t scan = a.bu_scan;
@@ -405,7 +512,7 @@ __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, co
         b[k] = __ldg(a.ioffs + v[k]);
         e[k] = __ldg(a.ioffs + v[k] + 1);
         lim[k] = min(e[k], b[k] + scan);
-        if (a.rep) r = __ldg(a.rep + v[k]);
+        if (use_rep && a.rep) r = __ldg(a.rep + v[k]);
       }
       found[k] = r != kNoRep && test_bit(fcur, r);
     }
@@ -451,7 +558,8 @@ __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, co
         const uint32_t w = v[k] >> 5, bit = 1u << (v[k] & 31u);
         atomicOr(a.visited + w, bit);
         atomicOr(fnext + w, bit);
-        a.depth[v[k]] = nd;
+        if (a.planes) mark_depth(a, w, bit, nd);
+        else a.depth[v[k]] = nd;
         nf += 1;
         mf += __ldg(a.offs + v[k] + 1) - __ldg(a.offs + v[k]);
       }
@@ -520,6 +628,8 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     uint32_t *bm = a.visited;
     const uint32_t words = (uint32_t)(a.front[2] - a.visited) + a.W;
     for (uint32_t i = gtid; i < words; i += nthreads) bm[i] = 0u;
+    if (a.planes)
+      for (uint32_t i = gtid; i < a.W; i += nthreads) a.planes[i] = 0u;
     if (gtid < 4 * sizeof(LevelSlot) / 4) ((uint32_t *)a.slots)[gtid] = 0u;
     if (gtid == 0 && a.ho) a.ho->flag = 0u;
   }
@@ -553,6 +663,14 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     // a pull level over bitmap words writes every word of fclr (its survivors)
     if (!(bu && surv == 0))
       for (uint32_t i = gtid; i < a.W; i += nthreads) fclr[i] = 0u;
+    // plane p is first written at level 2^p - 1 (depth 2^p): clear it now
+    if (a.planes && ((L + 2) & (L + 1)) == 0) {
+      const uint32_t p = 31 - __clz(L + 2);
+      if (p < a.nplanes) {
+        uint32_t *pl = a.planes + (size_t)p * a.Wp;
+        for (uint32_t i = gtid; i < a.W; i += nthreads) pl[i] = 0u;
+      }
+    }
     if (gtid < sizeof(LevelSlot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[gtid] = 0u;
     uint32_t nf = 0;
     unsigned long long mf = 0;
@@ -571,7 +689,17 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
       nf = vis.nf;
       mf = vis.mf;
     } else {
-      if (surv == 0) {
+      if (surv == 0 && a.rep) {
+        // the index pass over the words, then the vertices it left as a
+        // queue (their bitmap in fclr, cleared as it is read)
+        bu_level_rep<K>(a, L, fcur, fnext, nf, mf, fclr);
+        if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+        bitmap_to_queue(a, fclr, a.queue[L & 1u], &nx->dcount, true);
+        if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+        const uint32_t D = min(__ldcg(&nx->dcount), a.queue_cap);
+        bu_level_survivors<K>(a, L, fcur, fnext, a.queue[L & 1u], D, nf, mf,
+                              a.queue[(L + 1) & 1u], &nx->scount, false);
+      } else if (surv == 0) {
         uint32_t ns = 0;
         bu_level<K>(a, L, fcur, fnext, nf, mf, fclr, ns);
         const unsigned long long bns = block_sum_u64<kBlock>(ns);
@@ -621,12 +749,16 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
       // bfs_narrow (launched after this kernel).  Vertices unreached so far
       // read INFINIT now; the narrow kernel writes the depth of each vertex it
       // reaches later.
-      const uint32_t lane = lane_id();
-      const uint32_t gw = gtid >> 5, nw = nthreads >> 5;
-      for (uint32_t w = gw; w < a.W; w += nw) {
-        const uint32_t vis = __ldcg(a.visited + w);
-        const uint32_t v = w * 32 + lane;
-        if (!((vis >> lane) & 1u) && v < a.n) a.depth[v] = kInfinit;
+      if (a.planes) {
+        write_depths(a, 32 - __clz(L + 1));
+      } else {
+        const uint32_t lane = lane_id();
+        const uint32_t gw = gtid >> 5, nw = nthreads >> 5;
+        for (uint32_t w = gw; w < a.W; w += nw) {
+          const uint32_t vis = __ldcg(a.visited + w);
+          const uint32_t v = w * 32 + lane;
+          if (!((vis >> lane) & 1u) && v < a.n) a.depth[v] = kInfinit;
+        }
       }
       if (gtid == 0) {
         Handover *h = a.ho;
@@ -644,7 +776,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     }
     from_pull = bu && !nbu;
     // a push level after a word-based pull level still clears the bitmap
-    surv = !bu ? 0 : (surv == 0 ? 1 : 2);
+    surv = !bu ? 0 : (surv == 0 && !a.rep ? 1 : 2);
     if (!nbu && surv == 2) surv = 0;
     S = SN;
     if (nbu != bu) ++switches;
@@ -656,8 +788,10 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
       break;
     }
   }
-  // epilogue: unreached vertices read INFINIT
-  {
+  // epilogue: every depth from the planes, or INFINIT for unreached vertices
+  if (a.planes) {
+    write_depths(a, 32 - __clz(L));
+  } else {
     const uint32_t lane = lane_id();
     const uint32_t gw = gtid >> 5, nw = nthreads >> 5;
     for (uint32_t w = gw; w < a.W; w += nw) {
@@ -1038,6 +1172,9 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   a.front[0] = w->bitmaps + Wp;
   a.front[1] = w->bitmaps + 2 * Wp;
   a.front[2] = w->bitmaps + 3 * Wp;
+  a.planes = w->bitmaps + 4 * Wp;
+  a.Wp = (uint32_t)Wp;
+  a.nplanes = w->nplanes;
   a.queue[0] = w->queues;
   a.queue[1] = w->queues + g->n;
   a.chunks[0] = w->chunks;
