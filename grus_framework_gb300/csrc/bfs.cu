@@ -144,13 +144,23 @@ struct Args {
   uint64_t timeout_ns;
 };
 
+// Depth bit planes from this many vertices on.  Below it the depth array
+// stays in L2 (16 MB at 2^22 vertices), its partial-sector stores cost
+// little, and the planes' extra pass and atomics do not repay: best of 12
+// with the L2 flushed, stores against planes, RMAT scale 18 0.087 against
+// 0.099 ms, 21 0.130 against 0.136, 22 0.160 against 0.158, 23 0.267
+// against 0.211, 24 0.433 against 0.347.
+constexpr uint64_t kPlanesMinN = 1ull << 22;
+
 struct Workspace {
   uint64_t n = 0, m = 0;
   uint32_t W = 0;
   uint32_t *depth = nullptr;     // used when the caller's buffer is on the host
-  uint32_t *bitmaps = nullptr;   // visited + 3 fronts + depth planes, (4+P)*Wp words
+  uint32_t *bitmaps = nullptr;   // visited + 3 fronts (+ depth planes), (4[+P])*Wp words
   size_t bitmap_bytes = 0;       // the part kept in the L2 persisting window
   uint32_t nplanes = 0;          // P: bits of the largest possible depth
+  uint32_t *planes = nullptr;    // P*Wp words: after the fronts from kPlanesMinN
+  uint32_t *planes_own = nullptr;  // vertices on, else allocated when first asked for
   uint32_t *queues = nullptr;    // 2 * n
   uint4 *chunks = nullptr;       // 2 * chunk_cap
   uint32_t chunk_cap = 0;
@@ -174,6 +184,7 @@ void ws_free(void *p) {
   if (!w) return;
   cudaFree(w->depth);
   cudaFree(w->bitmaps);
+  cudaFree(w->planes_own);
   cudaFree(w->queues);
   cudaFree(w->chunks);
   cudaFree(w->ctrl);
@@ -200,13 +211,15 @@ int ws_get(grus_graph *g, Workspace **out) {
   uint32_t P = 1;
   while (P < 32 && (g->n >> P) != 0) ++P;
   w->nplanes = P;
-  w->bitmap_bytes = (4 + std::min<uint64_t>(P, 4)) * Wp * 4;
+  const bool with_planes = g->n >= kPlanesMinN;
+  w->bitmap_bytes = (4 + (with_planes ? std::min<uint64_t>(P, 4) : 0)) * Wp * 4;
   // chunk lists sized for any chunking degree down to 256 (the autotuner and
   // callers may lower it after the workspace exists)
   const uint32_t huge = std::min(tune_or(g->tuning.huge_degree, kDefHuge), 256u);
   const uint64_t cap = g->m / kChunk + g->m / std::max(huge, 1u) + 2;
   w->chunk_cap = (uint32_t)std::min<uint64_t>(cap, 0x7FFFFFFFull);
-  cudaError_t e = cudaMalloc(&w->bitmaps, (4 + (uint64_t)P) * Wp * 4);
+  cudaError_t e = cudaMalloc(&w->bitmaps, (4 + (with_planes ? (uint64_t)P : 0)) * Wp * 4);
+  if (e == cudaSuccess && with_planes) w->planes = w->bitmaps + 4 * Wp;
   if (e == cudaSuccess) e = cudaMalloc(&w->queues, 2 * std::max<uint64_t>(g->n, 1) * 4);
   if (e == cudaSuccess) e = cudaMalloc(&w->chunks, 2ull * w->chunk_cap * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
@@ -270,6 +283,7 @@ __device__ __noinline__ void write_depths(const Args &a, uint32_t np) {
 // ---------------------------------------------------------------------------
 // push level: visitor for expand_binned (expand.cuh)
 // ---------------------------------------------------------------------------
+template <bool P>
 struct PushVisitor {
   const Args *a;
   uint32_t nd;
@@ -289,7 +303,7 @@ struct PushVisitor {
     const uint32_t w = dst >> 5, bit = 1u << (dst & 31u);
     if (__ldcg(a->visited + w) & bit) return;
     if (atomicOr(a->visited + w, bit) & bit) return;
-    if (a->planes) mark_depth(*a, w, bit, nd);
+    if (P) mark_depth(*a, w, bit, nd);
     else a->depth[dst] = nd;
     atomicOr(fnext + w, bit);
     const uint32_t b = __ldg(a->offs + dst), e = __ldg(a->offs + dst + 1);
@@ -328,7 +342,7 @@ __device__ __forceinline__ void enqueue_binned(const Args &a, uint32_t v,
 // records its survivors as a bitmap (`sbm`, one plain store per word by the
 // warp that owns it: a queue append per word would put one atomic per word
 // on a single counter) and counts them in *scount.
-template <int K>
+template <int K, bool P>
 __device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32_t *fcur,
                                          uint32_t *fnext, uint32_t &nf, unsigned long long &mf,
                                          uint32_t *sbm, uint32_t &ns) {
@@ -409,10 +423,10 @@ __device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32
         if (lane == 0) {
           a.visited[w] = vis[k] | mask;
           fnext[w] = mask;
-          if (a.planes) mark_depth(a, w, mask, nd);
+          if (P) mark_depth(a, w, mask, nd);
         }
         if (found[k]) {
-          if (!a.planes) a.depth[v] = nd;
+          if (!P) a.depth[v] = nd;
           nf += 1;
           mf += __ldg(a.offs + v + 1) - __ldg(a.offs + v);
         }
@@ -434,7 +448,7 @@ __device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32
 // bu_level_survivors: with the probes of the few unresolved lanes removed
 // from the word pass, its steps no longer wait on the adjacency reads of one
 // or two lanes each.
-template <int K>
+template <int K, bool P>
 __device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const uint32_t *fcur,
                                              uint32_t *fnext, uint32_t &nf, unsigned long long &mf,
                                              uint32_t *dbm) {
@@ -461,7 +475,7 @@ __device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const ui
       const uint32_t dmask = __ballot_sync(0xffffffffu, r[k] != kNoRep && !found);
       const uint32_t w = w0 + k, v = w * 32 + lane;
       if (found) {
-        if (!a.planes) a.depth[v] = nd;
+        if (!P) a.depth[v] = nd;
         nf += 1;
         mf += e[k] - b[k];
       }
@@ -469,7 +483,7 @@ __device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const ui
         if (mask) {
           a.visited[w] = vis[k] | mask;
           fnext[w] = mask;
-          if (a.planes) mark_depth(a, w, mask, nd);
+          if (P) mark_depth(a, w, mask, nd);
         }
         dbm[w] = dmask;
       }
@@ -483,7 +497,7 @@ __device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const ui
 // are spread over warps, so found ones set their bits with atomics.  Those
 // still unresolved are appended to the next survivor queue, one reservation
 // per warp step.
-template <int K>
+template <int K, bool P>
 __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, const uint32_t *fcur,
                                                    uint32_t *fnext, const uint32_t *sin,
                                                    uint32_t S, uint32_t &nf, unsigned long long &mf,
@@ -558,7 +572,7 @@ __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, co
         const uint32_t w = v[k] >> 5, bit = 1u << (v[k] & 31u);
         atomicOr(a.visited + w, bit);
         atomicOr(fnext + w, bit);
-        if (a.planes) mark_depth(a, w, bit, nd);
+        if (P) mark_depth(a, w, bit, nd);
         else a.depth[v[k]] = nd;
         nf += 1;
         mf += __ldg(a.offs + v[k] + 1) - __ldg(a.offs + v[k]);
@@ -618,7 +632,8 @@ __device__ __forceinline__ void bitmap_to_queue(const Args &a, uint32_t *fmap, u
   }
 }
 
-template <int K>
+// P: depths as bit planes (Args::planes set) or stored as vertices are found
+template <int K, bool P>
 __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
@@ -628,7 +643,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     uint32_t *bm = a.visited;
     const uint32_t words = (uint32_t)(a.front[2] - a.visited) + a.W;
     for (uint32_t i = gtid; i < words; i += nthreads) bm[i] = 0u;
-    if (a.planes)
+    if (P)
       for (uint32_t i = gtid; i < a.W; i += nthreads) a.planes[i] = 0u;
     if (gtid < 4 * sizeof(LevelSlot) / 4) ((uint32_t *)a.slots)[gtid] = 0u;
     if (gtid == 0 && a.ho) a.ho->flag = 0u;
@@ -664,7 +679,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     if (!(bu && surv == 0))
       for (uint32_t i = gtid; i < a.W; i += nthreads) fclr[i] = 0u;
     // plane p is first written at level 2^p - 1 (depth 2^p): clear it now
-    if (a.planes && ((L + 2) & (L + 1)) == 0) {
+    if (P && ((L + 2) & (L + 1)) == 0) {
       const uint32_t p = 31 - __clz(L + 2);
       if (p < a.nplanes) {
         uint32_t *pl = a.planes + (size_t)p * a.Wp;
@@ -675,7 +690,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     uint32_t nf = 0;
     unsigned long long mf = 0;
     if (!bu) {
-      PushVisitor vis{&a, L + 1, fnext, a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx, 0u, 0ull};
+      PushVisitor<P> vis{&a, L + 1, fnext, a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx, 0u, 0ull};
       if (from_pull) {
         bitmap_to_queue(a, fcur, a.queue[L & 1u], &cur->qcount);
         // survivors recorded as a bitmap sit in this level's next frontier
@@ -692,16 +707,16 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
       if (surv == 0 && a.rep) {
         // the index pass over the words, then the vertices it left as a
         // queue (their bitmap in fclr, cleared as it is read)
-        bu_level_rep<K>(a, L, fcur, fnext, nf, mf, fclr);
+        bu_level_rep<K, P>(a, L, fcur, fnext, nf, mf, fclr);
         if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
         bitmap_to_queue(a, fclr, a.queue[L & 1u], &nx->dcount, true);
         if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
         const uint32_t D = min(__ldcg(&nx->dcount), a.queue_cap);
-        bu_level_survivors<K>(a, L, fcur, fnext, a.queue[L & 1u], D, nf, mf,
+        bu_level_survivors<K, P>(a, L, fcur, fnext, a.queue[L & 1u], D, nf, mf,
                               a.queue[(L + 1) & 1u], &nx->scount, false);
       } else if (surv == 0) {
         uint32_t ns = 0;
-        bu_level<K>(a, L, fcur, fnext, nf, mf, fclr, ns);
+        bu_level<K, P>(a, L, fcur, fnext, nf, mf, fclr, ns);
         const unsigned long long bns = block_sum_u64<kBlock>(ns);
         if (threadIdx.x == 0 && bns) atomicAdd(&nx->scount, (uint32_t)bns);
       } else {
@@ -712,7 +727,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
           if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
           S = min(__ldcg(&cur->qcount), a.queue_cap);
         }
-        bu_level_survivors<K>(a, L, fcur, fnext, a.queue[L & 1u], S, nf, mf,
+        bu_level_survivors<K, P>(a, L, fcur, fnext, a.queue[L & 1u], S, nf, mf,
                               a.queue[(L + 1) & 1u], &nx->scount);
       }
     }
@@ -749,7 +764,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
       // bfs_narrow (launched after this kernel).  Vertices unreached so far
       // read INFINIT now; the narrow kernel writes the depth of each vertex it
       // reaches later.
-      if (a.planes) {
+      if (P) {
         write_depths(a, 32 - __clz(L + 1));
       } else {
         const uint32_t lane = lane_id();
@@ -789,7 +804,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     }
   }
   // epilogue: every depth from the planes, or INFINIT for unreached vertices
-  if (a.planes) {
+  if (P) {
     write_depths(a, 32 - __clz(L));
   } else {
     const uint32_t lane = lane_id();
@@ -1131,9 +1146,12 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   // pull-level words per warp step: 2 (more resident warps) or 4 (more
   // loads in flight per warp)
   const bool wide = tune_or(g->tuning.bu_words, kDefBuWords) >= 4;
-  auto kern = wide ? bfs_persistent<4> : bfs_persistent<2>;
-  static int occ_tab[2] = {-1, -1};
-  int &occ = occ_tab[wide ? 1 : 0];
+  const uint32_t pmode = g->tuning.depth_planes;
+  const bool planes = pmode == 1 || (pmode == 0 && g->n >= kPlanesMinN);
+  auto kern = wide ? (planes ? bfs_persistent<4, true> : bfs_persistent<4, false>)
+                   : (planes ? bfs_persistent<2, true> : bfs_persistent<2, false>);
+  static int occ_tab[4] = {-1, -1, -1, -1};
+  int &occ = occ_tab[(wide ? 2 : 0) + (planes ? 1 : 0)];
   if (occ < 0) {
     GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kBlock, 0));
   }
@@ -1172,7 +1190,13 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   a.front[0] = w->bitmaps + Wp;
   a.front[1] = w->bitmaps + 2 * Wp;
   a.front[2] = w->bitmaps + 3 * Wp;
-  a.planes = w->bitmaps + 4 * Wp;
+  if (planes) {
+    if (!w->planes) {
+      GRUS_CUDA_TRY(cudaMalloc(&w->planes_own, (uint64_t)w->nplanes * Wp * 4));
+      w->planes = w->planes_own;
+    }
+    a.planes = w->planes;
+  }
   a.Wp = (uint32_t)Wp;
   a.nplanes = w->nplanes;
   a.queue[0] = w->queues;
@@ -1377,7 +1401,7 @@ int static_scratch(void **base, int *occ) {
       return status_from_cuda(rc == cudaSuccess ? cudaErrorInvalidSymbol : rc);
     }
     int o = 0;
-    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, bfs_persistent<4>, kBlock, 0));
+    GRUS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, bfs_persistent<4, false>, kBlock, 0));
     e.ctx = ctx;
     e.base = p;
     e.occ = std::max(o, 1);
@@ -1462,7 +1486,7 @@ extern "C" int grus_bfs_static(uint64_t n, uint64_t m, const uint32_t *offsets,
   cfg.stream = s;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
-  GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, bfs_persistent<4>, a));
+  GRUS_CUDA_TRY(cudaLaunchKernelEx(&cfg, bfs_persistent<4, false>, a));
   if (!stats) return GRUS_OK;
   unsigned char host_ctrl[kCtrlBytes];  // pageable stack copy: no allocation
   GRUS_CUDA_TRY(cudaMemcpyAsync(host_ctrl, ctrl, kCtrlBytes, cudaMemcpyDeviceToHost, s));

@@ -48,6 +48,7 @@ extern "C" int grus_autotune(grus_graph *g, uint32_t algo, uint32_t src, int rep
     knobs.push_back({nullptr, &grus_tuning::alpha, {6, 15, 40}});
     knobs.push_back({nullptr, &grus_tuning::beta, {8, 18, 48}});
     knobs.push_back({&grus_tuning::bu_words, nullptr, {2, 4}});
+    knobs.push_back({&grus_tuning::depth_planes, nullptr, {1, 2}});
     knobs.push_back({&grus_tuning::huge_degree, nullptr, {512, 1024, 4096}});
     knobs.push_back({&grus_tuning::ctas_per_sm, nullptr, {0, 2, 3}});
   } else {

@@ -112,6 +112,10 @@ typedef struct grus_tuning {
   float multi_alpha;      /* multi-source BFS: push->pull when the union frontier's
                              out-edges exceed m / multi_alpha (0: 10 up to 32
                              sources, 6 above) */
+  uint32_t depth_planes;  /* BFS: keep depths as bit planes in L2 and write the
+                             depth array once at the end (1), or store each
+                             depth as its vertex is found (2); 0: planes from
+                             2^22 vertices on */
 } grus_tuning;
 
 /* ---- library ------------------------------------------------------------- */

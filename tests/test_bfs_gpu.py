@@ -223,3 +223,40 @@ def test_bfs_pull_index(grus, oracle_mod):
         if sym:
             assert st["bottom_up_levels"] >= 1
         g.free()
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_bfs_depth_planes(grus, oracle_mod, mode):
+    """Depths kept as bit planes and written out at the end (1) or stored as
+    vertices are found (2), forced on graphs below the automatic threshold:
+    pull-heavy and push-only schedules, a directed graph with its CSC, a grid
+    whose traversal hands over to the cluster tail (the planes are written
+    out at the hand-over), and long tails with a spilling hub and sinks."""
+    g = grus.Graph.rmat(15, 16, 7, symmetric=True)
+    for alpha, beta in ((1e9, 18.0), (1e-6, 1e9), (15.0, 18.0)):
+        g.set_tuning(alpha=alpha, beta=beta, depth_planes=mode)
+        _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, 5])
+    g.free()
+    g = grus.Graph.rmat(14, 16, 3, symmetric=False)
+    g.build_csc()
+    g.set_tuning(alpha=2.0, beta=1e9, depth_planes=mode)
+    _check_bfs(grus, oracle_mod, g, [g.max_degree_vertex, 999])
+    g.free()
+    g = grus.Graph.grid2d(300, 200)
+    g.set_tuning(depth_planes=mode)
+    _check_bfs(grus, oracle_mod, g, [201, 59999])
+    g.free()
+    offs, cols = _broom(200, 100000)
+    g = grus.Graph.from_csr(offs, cols, symmetric=True)
+    g.set_tuning(depth_planes=mode)
+    _check_bfs(grus, oracle_mod, g, [0, 199])
+    g.free()
+
+
+def test_bfs_depth_planes_tuning_range(grus):
+    g = grus.Graph.rmat(8, 4, 1)
+    with pytest.raises(grus.GrusError):
+        g.set_tuning(depth_planes=3)
+    g.set_tuning(depth_planes=0)
+    assert g.get_tuning()["depth_planes"] == 0
+    g.free()
