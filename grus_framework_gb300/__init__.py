@@ -115,7 +115,7 @@ class Tuning(C.Structure):
         ("alpha", C.c_float), ("beta", C.c_float), ("ctas_per_sm", C.c_uint32),
         ("huge_degree", C.c_uint32), ("bu_scan", C.c_uint32), ("timeout_ms", C.c_uint32),
         ("sssp_delta", C.c_uint32), ("bu_words", C.c_uint32), ("multi_alpha", C.c_float),
-        ("depth_planes", C.c_uint32),
+        ("depth_planes", C.c_uint32), ("tail_cluster", C.c_uint32),
     ]
 
 

@@ -250,32 +250,75 @@ __device__ __forceinline__ void mark_depth(const Args &a, uint32_t w, uint32_t m
 }
 
 // Writes every vertex's depth from the bit planes of depths below 2^np and
-// the visited bitmap (unreached: INFINIT): a warp turns K words into K whole
-// 128-byte lines of the depth array per step.
-__device__ __noinline__ void write_depths(const Args &a, uint32_t np) {
-  constexpr int KM = 4;
+// the visited bitmap (unreached: INFINIT).  A warp takes 32 consecutive
+// words (1,024 vertices): lane j loads word j of the visited map and of each
+// plane, one coalesced request per map, so a step waits for one L2 round
+// trip.  Then, eight times, each lane takes four consecutive vertices (bits
+// 4(j mod 8) .. +3 of word 4i + j/8, read from its owner lane by a shuffle)
+// and stores their depths as one 16-byte word: 512 contiguous bytes per
+// warp store.  Two slower forms measured at RMAT-24 (np = 3): lane = vertex
+// with the planes read one after another, 1 + np round trips per 8 words
+// (62 us); the same with all loads of a step issued together (71 us, the
+// loads queued behind the stores).
+template <int NP>
+__device__ __forceinline__ void write_depths_np(const Args &a, uint32_t np) {
   const uint32_t lane = lane_id();
   const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * kBlock) >> 5;
-  for (uint32_t w0 = gw * KM; w0 < a.W; w0 += nw * KM) {
-    uint32_t vis[KM], d[KM];
+  const bool vec = ((uintptr_t)a.depth & 15u) == 0;
+  const uint32_t sh = 4 * (lane & 7u);
+  for (uint32_t w0 = gw * 32; w0 < a.W; w0 += nw * 32) {
+    const uint32_t w = w0 + lane;
+    const bool ok = w < a.W;
+    const uint32_t vis = ok ? __ldcg(a.visited + w) : 0u;
+    uint32_t pw[NP];
 #pragma unroll
-    for (int k = 0; k < KM; ++k) {
-      vis[k] = w0 + k < a.W ? __ldcg(a.visited + w0 + k) : 0u;
-      d[k] = 0u;
-    }
-    for (uint32_t p = 0; p < np; ++p) {
-      const uint32_t *pl = a.planes + (size_t)p * a.Wp;
+    for (int p = 0; p < NP; ++p)
+      pw[p] = ok && (uint32_t)p < np ? __ldcg(a.planes + (size_t)p * a.Wp + w) : 0u;
+#pragma unroll 2
+    for (int i = 0; i < 8; ++i) {
+      const int t = i * 4 + (int)(lane >> 3);
+      const uint32_t vt = __shfl_sync(0xffffffffu, vis, t) >> sh;
+      uint32_t nib[NP];
 #pragma unroll
-      for (int k = 0; k < KM; ++k) {
-        const uint32_t pw = w0 + k < a.W ? __ldcg(pl + w0 + k) : 0u;
-        d[k] |= ((pw >> lane) & 1u) << p;
+      for (int p = 0; p < NP; ++p) nib[p] = __shfl_sync(0xffffffffu, pw[p], t) >> sh;
+      uint32_t o[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        uint32_t d = 0u;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) d |= ((nib[p] >> e) & 1u) << p;
+        o[e] = ((vt >> e) & 1u) ? d : kInfinit;
+      }
+      if (w0 + t >= a.W) continue;
+      const uint64_t v0 = (uint64_t)(w0 + t) * 32 + sh;
+      if (vec && v0 + 4 <= a.n) {
+        *reinterpret_cast<uint4 *>(a.depth + v0) = make_uint4(o[0], o[1], o[2], o[3]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (v0 + e < a.n) a.depth[v0 + e] = o[e];
       }
     }
-#pragma unroll
-    for (int k = 0; k < KM; ++k) {
-      const uint32_t v = (w0 + k) * 32 + lane;
-      if (w0 + k < a.W && v < a.n) a.depth[v] = ((vis[k] >> lane) & 1u) ? d[k] : kInfinit;
+  }
+}
+
+__device__ __noinline__ void write_depths(const Args &a, uint32_t np) {
+  if (np <= 4) write_depths_np<4>(a, np);
+  else if (np <= 8) write_depths_np<8>(a, np);
+  else if (np <= 16) write_depths_np<16>(a, np);
+  else {
+    // depths of 65,536 and more: a word per warp step
+    const uint32_t lane = lane_id();
+    const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * kBlock) >> 5;
+    for (uint32_t w = gw; w < a.W; w += nw) {
+      const uint32_t vis = __ldcg(a.visited + w);
+      uint32_t d = 0u;
+      for (uint32_t p = 0; p < np; ++p)
+        d |= ((__ldcg(a.planes + (size_t)p * a.Wp + w) >> lane) & 1u) << p;
+      const uint32_t v = w * 32 + lane;
+      if (v < a.n) a.depth[v] = ((vis >> lane) & 1u) ? d : kInfinit;
     }
   }
 }
@@ -1216,7 +1259,7 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   a.bu_scan = tune_or(g->tuning.bu_scan,
                       g->mem_mode == GRUS_MEM_MANAGED ? kDefBuScanManaged : kDefBuScan);
   const int ncl = narrow_cluster();
-  a.narrow_nf = kNarrowNf * (uint32_t)ncl;
+  a.narrow_nf = g->tuning.tail_cluster == 2 ? 0u : kNarrowNf * (uint32_t)ncl;
   a.ho = (Handover *)(w->ctrl + kOffHandover);
   a.timeout_ns = (uint64_t)tune_or(g->tuning.timeout_ms, 30000u) * 1000000ull;
 

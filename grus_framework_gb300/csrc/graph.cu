@@ -792,7 +792,7 @@ int grus_graph_build_index(grus_graph *g, float *build_ms) {
 int grus_graph_set_tuning(grus_graph *g, const grus_tuning *t) {
   if (!g || !t) return GRUS_EINVAL;
   if (t->alpha < 0.f || t->beta < 0.f || t->multi_alpha < 0.f || t->ctas_per_sm > 64 ||
-      t->depth_planes > 2)
+      t->depth_planes > 2 || t->tail_cluster > 2)
     return GRUS_EINVAL;
   std::lock_guard<std::mutex> lk(g->mu);
   if (t->huge_degree != g->tuning.huge_degree) {

@@ -116,6 +116,10 @@ typedef struct grus_tuning {
                              depth array once at the end (1), or store each
                              depth as its vertex is found (2); 0: planes from
                              2^22 vertices on */
+  uint32_t tail_cluster;  /* BFS: hand a long traversal whose push frontier has
+                             become small to the thread-block-cluster tail (0
+                             or 1), or run every level in the persistent
+                             kernel (2) */
 } grus_tuning;
 
 /* ---- library ------------------------------------------------------------- */

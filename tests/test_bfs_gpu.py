@@ -255,8 +255,38 @@ def test_bfs_depth_planes(grus, oracle_mod, mode):
 
 def test_bfs_depth_planes_tuning_range(grus):
     g = grus.Graph.rmat(8, 4, 1)
-    with pytest.raises(grus.GrusError):
-        g.set_tuning(depth_planes=3)
-    g.set_tuning(depth_planes=0)
-    assert g.get_tuning()["depth_planes"] == 0
+    for field in ("depth_planes", "tail_cluster"):
+        with pytest.raises(grus.GrusError):
+            g.set_tuning(**{field: 3})
+        g.set_tuning(**{field: 0})
+        assert g.get_tuning()[field] == 0
+    g.free()
+
+
+def _path(n):
+    """A symmetric path 0 - 1 - ... - n-1."""
+    deg = np.full(n, 2, np.int64)
+    deg[0] = deg[-1] = 1
+    offs = np.zeros(n + 1, np.uint32)
+    offs[1:] = np.cumsum(deg)
+    cols = np.empty(int(offs[-1]), np.uint32)
+    cols[offs[1:-1] - 1] = np.arange(1, n, dtype=np.uint32)        # right neighbour, last slot
+    cols[offs[1:-1]] = np.arange(0, n - 1, dtype=np.uint32)        # left neighbour, first slot
+    return offs, cols
+
+
+@pytest.mark.parametrize("n,src", [(300 * 200, None), (70001, 0)])
+def test_bfs_depth_planes_deep(grus, oracle_mod, n, src):
+    """Every level in the persistent kernel (no cluster tail), so the planes
+    hold depths of up to 9 bits (a 300 x 200 grid) and of 17 bits (a path of
+    70,001 vertices, depths up to 70,000): the closing pass's wider forms."""
+    if src is None:
+        g = grus.Graph.grid2d(300, 200)
+        srcs = [201, 59999]
+    else:
+        offs, cols = _path(n)
+        g = grus.Graph.from_csr(offs, cols, symmetric=True)
+        srcs = [src, n // 3]
+    g.set_tuning(depth_planes=1, tail_cluster=2)
+    _check_bfs(grus, oracle_mod, g, srcs)
     g.free()
