@@ -128,6 +128,8 @@ struct Args {
   uint32_t *planes;
   uint32_t Wp, nplanes;
   uint32_t *visited;      // W words; fronts follow contiguously
+  uint32_t *aux;          // W words, with the pull index: the index pass's
+                          // unresolved vertices of in-degree one
   uint32_t *front[3];
   uint32_t *queue[2];
   uint4 *chunks[2];
@@ -156,7 +158,7 @@ struct Workspace {
   uint64_t n = 0, m = 0;
   uint32_t W = 0;
   uint32_t *depth = nullptr;     // used when the caller's buffer is on the host
-  uint32_t *bitmaps = nullptr;   // visited + 3 fronts (+ depth planes), (4[+P])*Wp words
+  uint32_t *bitmaps = nullptr;   // visited + 3 fronts + aux (+ depth planes), (5[+P])*Wp words
   size_t bitmap_bytes = 0;       // the part kept in the L2 persisting window
   uint32_t nplanes = 0;          // P: bits of the largest possible depth
   uint32_t *planes = nullptr;    // P*Wp words: after the fronts from kPlanesMinN
@@ -212,14 +214,14 @@ int ws_get(grus_graph *g, Workspace **out) {
   while (P < 32 && (g->n >> P) != 0) ++P;
   w->nplanes = P;
   const bool with_planes = g->n >= kPlanesMinN;
-  w->bitmap_bytes = (4 + (with_planes ? std::min<uint64_t>(P, 4) : 0)) * Wp * 4;
+  w->bitmap_bytes = (5 + (with_planes ? std::min<uint64_t>(P, 4) : 0)) * Wp * 4;
   // chunk lists sized for any chunking degree down to 256 (the autotuner and
   // callers may lower it after the workspace exists)
   const uint32_t huge = std::min(tune_or(g->tuning.huge_degree, kDefHuge), 256u);
   const uint64_t cap = g->m / kChunk + g->m / std::max(huge, 1u) + 2;
   w->chunk_cap = (uint32_t)std::min<uint64_t>(cap, 0x7FFFFFFFull);
-  cudaError_t e = cudaMalloc(&w->bitmaps, (4 + (with_planes ? (uint64_t)P : 0)) * Wp * 4);
-  if (e == cudaSuccess && with_planes) w->planes = w->bitmaps + 4 * Wp;
+  cudaError_t e = cudaMalloc(&w->bitmaps, (5 + (with_planes ? (uint64_t)P : 0)) * Wp * 4);
+  if (e == cudaSuccess && with_planes) w->planes = w->bitmaps + 5 * Wp;
   if (e == cudaSuccess) e = cudaMalloc(&w->queues, 2 * std::max<uint64_t>(g->n, 1) * 4);
   if (e == cudaSuccess) e = cudaMalloc(&w->chunks, 2ull * w->chunk_cap * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc(&w->ctrl, kCtrlBytes);
@@ -496,6 +498,8 @@ __device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const ui
                                              uint32_t *fnext, uint32_t &nf, unsigned long long &mf,
                                              uint32_t *dbm) {
   const uint32_t nd = L + 1;
+  // in-degree = out-degree on a symmetric graph (in-edges are the CSR)
+  const bool sym = a.ioffs == a.offs;
   const uint32_t lane = lane_id();
   const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * kBlock) >> 5;
@@ -515,7 +519,12 @@ __device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const ui
     for (int k = 0; k < K; ++k) {
       const bool found = r[k] != kNoRep && test_bit(fcur, r[k]);
       const uint32_t mask = __ballot_sync(0xffffffffu, found);
-      const uint32_t dmask = __ballot_sync(0xffffffffu, r[k] != kNoRep && !found);
+      // a vertex whose one in-neighbour is its representative is resolved:
+      // it survives to the next level without a probe
+      const bool unres = r[k] != kNoRep && !found;
+      const bool one = sym && e[k] - b[k] == 1u;
+      const uint32_t dmask = __ballot_sync(0xffffffffu, unres && !one);
+      const uint32_t smask = __ballot_sync(0xffffffffu, unres && one);
       const uint32_t w = w0 + k, v = w * 32 + lane;
       if (found) {
         if (!P) a.depth[v] = nd;
@@ -529,6 +538,7 @@ __device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const ui
           if (P) mark_depth(a, w, mask, nd);
         }
         dbm[w] = dmask;
+        a.aux[w] = smask;
       }
     }
   }
@@ -675,6 +685,44 @@ __device__ __forceinline__ void bitmap_to_queue(const Args &a, uint32_t *fmap, u
   }
 }
 
+// bitmap_to_queue over two maps at once, one block scan of both counts
+// (packed in 16-bit halves: at most 256 x 32 per block): m1 is cleared as it
+// is read, m2 is left as it is.
+__device__ __forceinline__ void bitmaps_to_queues(const Args &a, uint32_t *m1, uint32_t *q1,
+                                                  uint32_t *c1, const uint32_t *m2, uint32_t *q2,
+                                                  uint32_t *c2) {
+  __shared__ uint32_t s_base[2];
+  const uint32_t per = (a.W + gridDim.x - 1) / gridDim.x;
+  const uint32_t w0 = blockIdx.x * per, w1 = min(a.W, w0 + per);
+  for (uint32_t base = w0; base < w1; base += kBlock) {
+    const uint32_t w = base + threadIdx.x;
+    uint32_t x1 = w < w1 ? __ldcg(m1 + w) : 0u;
+    uint32_t x2 = w < w1 ? __ldcg(m2 + w) : 0u;
+    if (x1) m1[w] = 0u;
+    uint32_t total = 0;
+    const uint32_t at = block_exclusive_scan<kBlock>(__popc(x1) | (__popc(x2) << 16), &total);
+    if (threadIdx.x == 0) {
+      if (total & 0xFFFFu) s_base[0] = atomicAdd(c1, total & 0xFFFFu);
+      if (total >> 16) s_base[1] = atomicAdd(c2, total >> 16);
+    }
+    __syncthreads();
+    if (!total) continue;
+    uint32_t at1 = s_base[0] + (at & 0xFFFFu), at2 = s_base[1] + (at >> 16);
+    while (x1) {
+      const int bit = __ffs(x1) - 1;
+      x1 &= x1 - 1;
+      if (at1 < a.queue_cap) q1[at1] = w * 32 + bit;
+      ++at1;
+    }
+    while (x2) {
+      const int bit = __ffs(x2) - 1;
+      x2 &= x2 - 1;
+      if (at2 < a.queue_cap) q2[at2] = w * 32 + bit;
+      ++at2;
+    }
+  }
+}
+
 // P: depths as bit planes (Args::planes set) or stored as vertices are found
 template <int K, bool P>
 __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
@@ -750,9 +798,16 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
       if (surv == 0 && a.rep) {
         // the index pass over the words, then the vertices it left as a
         // queue (their bitmap in fclr, cleared as it is read)
-        bu_level_rep<K, P>(a, L, fcur, fnext, nf, mf, fclr);
+        // twice the words per warp step of the probing passes: this pass
+        // holds four registers per word (RMAT-24: 8 words 85 us, 4 words
+        // 110 us, 12 or 16 words 142 us)
+        bu_level_rep<2 * K, P>(a, L, fcur, fnext, nf, mf, fclr);
         if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-        bitmap_to_queue(a, fclr, a.queue[L & 1u], &nx->dcount, true);
+        // the vertices to probe as this level's queue; those of in-degree
+        // one start the next level's survivor queue, which the probe pass
+        // appends to
+        bitmaps_to_queues(a, fclr, a.queue[L & 1u], &nx->dcount, a.aux, a.queue[(L + 1) & 1u],
+                          &nx->scount);
         if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
         const uint32_t D = min(__ldcg(&nx->dcount), a.queue_cap);
         bu_level_survivors<K, P>(a, L, fcur, fnext, a.queue[L & 1u], D, nf, mf,
@@ -1233,6 +1288,7 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
   a.front[0] = w->bitmaps + Wp;
   a.front[1] = w->bitmaps + 2 * Wp;
   a.front[2] = w->bitmaps + 3 * Wp;
+  a.aux = w->bitmaps + 4 * Wp;
   if (planes) {
     if (!w->planes) {
       GRUS_CUDA_TRY(cudaMalloc(&w->planes_own, (uint64_t)w->nplanes * Wp * 4));
