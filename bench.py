@@ -436,9 +436,9 @@ def run_grus(args, dist, rank, local):
     # first call, like the graph itself; its build time goes into the line
     index = None
     if algo == "bfs" and (w.get("symmetric", True) or w["graph"] == "grid"):
-        index = {"bytes": 4 * n, "build_ms": round(g.build_index(), 3),
-                 "what": "per vertex, an in-neighbour of high out-degree, tested before the "
-                         "vertex's adjacency in pull levels"}
+        index = {"bytes": 8 * n, "build_ms": round(g.build_index(), 3),
+                 "what": "per vertex, an in-neighbour of high out-degree and the vertex's "
+                         "out-degree, tested before the vertex's adjacency in pull levels"}
     out_dev = make_out(False)
     _, st = call(out_dev, stats=True)
     nr, mr = st["vertices_reached"], st["edges_reached"]

@@ -114,7 +114,7 @@ struct Args {
   const uint32_t *__restrict__ cols;
   const uint32_t *__restrict__ ioffs;  // in-edges (pull levels): the CSR itself
   const uint32_t *__restrict__ icols;  // on a symmetric graph, else the CSC
-  const uint32_t *__restrict__ rep;    // pull index (null: none), grus_graph::bfs_rep
+  const uint2 *__restrict__ rep;       // pull index {rep, out-degree} (null: none), grus_graph::bfs_rep
   bool allow_pull;                     // false when no in-edge arrays exist
   uint32_t n, W;
   uint64_t m;
@@ -241,6 +241,11 @@ int ws_get(grus_graph *g, Workspace **out) {
   g->ws_free[kWsBfs] = ws_free;
   *out = w;
   return GRUS_OK;
+}
+
+// The representatives alone: word 2v of the index.
+__device__ __forceinline__ const uint32_t *rep_ids(const Args &a) {
+  return reinterpret_cast<const uint32_t *>(a.rep);
 }
 
 // Records depth nd for the vertices of `mask` in word w: one non-returning
@@ -413,13 +418,12 @@ __device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32
         lim[k] = min(e[k], b[k] + scan);
       }
     }
-    // the representative in-neighbour first (coalesced); only vertices it
-    // does not settle read their adjacency below
+    // with the pull index: the representative in-neighbour first (coalesced)
     if (a.rep) {
 #pragma unroll
       for (int k = 0; k < K; ++k) {
         const uint32_t v = (w0 + k) * 32 + lane;
-        const uint32_t r = act[k] ? __ldg(a.rep + v) : kNoRep;
+        const uint32_t r = act[k] ? __ldg(rep_ids(a) + 2 * (size_t)v) : kNoRep;
         found[k] = r != kNoRep && test_bit(fcur, r);
       }
     }
@@ -504,16 +508,23 @@ __device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const ui
   const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * kBlock) >> 5;
   for (uint32_t w0 = gw * K; w0 < a.W; w0 += nw * K) {
-    uint32_t vis[K], r[K], b[K], e[K];
+    uint32_t vis[K], r[K], dg[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) vis[k] = w0 + k < a.W ? __ldcg(a.visited + w0 + k) : 0xFFFFFFFFu;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       const uint32_t v = (w0 + k) * 32 + lane;
       const bool act = !((vis[k] >> lane) & 1u) && v < a.n;
-      r[k] = act ? __ldg(a.rep + v) : kNoRep;
-      b[k] = act ? __ldg(a.offs + v) : 0u;
-      e[k] = act ? __ldg(a.offs + v + 1) : 0u;
+      if constexpr (P) {
+        const uint2 rd = act ? __ldg(a.rep + v) : make_uint2(kNoRep, 0u);
+        r[k] = rd.x;
+        dg[k] = rd.y;
+      } else {
+        // graphs below the planes threshold: this form keeps the stores
+        // kernel free of spills (the index entry's degree is not used)
+        r[k] = act ? __ldg(rep_ids(a) + 2 * (size_t)v) : kNoRep;
+        dg[k] = act ? __ldg(a.offs + v + 1) - __ldg(a.offs + v) : 0u;
+      }
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -522,14 +533,14 @@ __device__ __forceinline__ void bu_level_rep(const Args &a, uint32_t L, const ui
       // a vertex whose one in-neighbour is its representative is resolved:
       // it survives to the next level without a probe
       const bool unres = r[k] != kNoRep && !found;
-      const bool one = sym && e[k] - b[k] == 1u;
+      const bool one = sym && dg[k] == 1u;
       const uint32_t dmask = __ballot_sync(0xffffffffu, unres && !one);
       const uint32_t smask = __ballot_sync(0xffffffffu, unres && one);
       const uint32_t w = w0 + k, v = w * 32 + lane;
       if (found) {
         if (!P) a.depth[v] = nd;
         nf += 1;
-        mf += e[k] - b[k];
+        mf += dg[k];
       }
       if (lane == 0 && w < a.W) {
         if (mask) {
@@ -570,18 +581,42 @@ __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, co
       act[k] = i < S;
       v[k] = act[k] ? __ldcg(sin + i) : 0u;
     }
+    const bool idx = use_rep && a.rep;
+    // P (big graphs): a vertex the index settles adds its out-degree from its
+    // entry here, and only the others read their offsets (a random vertex's
+    // offsets are one more sector from HBM); one found by a probe reads its
+    // out-degree below.  Otherwise offsets and representative load together.
+    const bool early_mf = P && idx;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       found[k] = false;
       b[k] = e[k] = lim[k] = 0;
-      uint32_t r = kNoRep;
-      if (act[k]) {
-        b[k] = __ldg(a.ioffs + v[k]);
-        e[k] = __ldg(a.ioffs + v[k] + 1);
-        lim[k] = min(e[k], b[k] + scan);
-        if (use_rep && a.rep) r = __ldg(a.rep + v[k]);
+      if constexpr (P) {
+        if (idx && act[k]) {
+          const uint2 rd = __ldg(a.rep + v[k]);
+          found[k] = rd.x != kNoRep && test_bit(fcur, rd.x);
+          if (found[k]) mf += rd.y;
+        }
+      } else {
+        uint32_t r = kNoRep;
+        if (act[k]) {
+          b[k] = __ldg(a.ioffs + v[k]);
+          e[k] = __ldg(a.ioffs + v[k] + 1);
+          lim[k] = min(e[k], b[k] + scan);
+          if (idx) r = __ldg(rep_ids(a) + 2 * (size_t)v[k]);
+        }
+        found[k] = r != kNoRep && test_bit(fcur, r);
       }
-      found[k] = r != kNoRep && test_bit(fcur, r);
+    }
+    if constexpr (P) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (act[k] && !found[k]) {
+          b[k] = __ldg(a.ioffs + v[k]);
+          e[k] = __ldg(a.ioffs + v[k] + 1);
+          lim[k] = min(e[k], b[k] + scan);
+        }
+      }
     }
     for (uint32_t r = 0; r < scan; r += 4) {
       uint32_t u[K][4];
@@ -623,12 +658,13 @@ __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, co
       }
       if (found[k]) {
         const uint32_t w = v[k] >> 5, bit = 1u << (v[k] & 31u);
+        // probed (b < e): the index did not settle it
         atomicOr(a.visited + w, bit);
         atomicOr(fnext + w, bit);
         if (P) mark_depth(a, w, bit, nd);
         else a.depth[v[k]] = nd;
         nf += 1;
-        mf += __ldg(a.offs + v[k] + 1) - __ldg(a.offs + v[k]);
+        if (!early_mf || b[k] < e[k]) mf += __ldg(a.offs + v[k] + 1) - __ldg(a.offs + v[k]);
       }
     }
     uint32_t m[K], tot = 0;
@@ -795,7 +831,10 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
       nf = vis.nf;
       mf = vis.mf;
     } else {
-      if (surv == 0 && a.rep) {
+      // the two-pass form with the index on big graphs (the planes form);
+      // below that the word pass tests the representative itself: at RMAT
+      // scales 16-20 its barrier and conversion cost more than they save
+      if (surv == 0 && a.rep && P) {
         // the index pass over the words, then the vertices it left as a
         // queue (their bitmap in fclr, cleared as it is read)
         // twice the words per warp step of the probing passes: this pass
@@ -889,7 +928,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     }
     from_pull = bu && !nbu;
     // a push level after a word-based pull level still clears the bitmap
-    surv = !bu ? 0 : (surv == 0 && !a.rep ? 1 : 2);
+    surv = !bu ? 0 : (surv == 0 && !(a.rep && P) ? 1 : 2);
     if (!nbu && surv == 2) surv = 0;
     S = SN;
     if (nbu != bu) ++switches;

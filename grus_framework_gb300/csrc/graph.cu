@@ -340,8 +340,11 @@ int graph_from_host(uint64_t n, uint64_t m, const uint32_t *offs,
   return GRUS_OK;
 }
 
-// rep[v]: among the first kRepScan in-neighbours of v, one of largest
-// out-degree (the first such), or kNoRep.  One warp per vertex; the key
+// rep[v].x: among the first kRepScan in-neighbours of v, one of largest
+// out-degree (the first such), or kNoRep; rep[v].y: v's out-degree, so one
+// 8-byte load gives a pull level both the test and the frontier's edge
+// count (a random vertex's entry is one sector, where the representative
+// and the offsets were two).  One warp per vertex; the key
 // (out-degree, -position) is reduced across the lanes.  A BFS pull level tests
 // this vertex's frontier bit before reading v's adjacency: high-degree
 // neighbours are reached early, so for nearly every vertex found at a pull
@@ -350,7 +353,7 @@ int graph_from_host(uint64_t n, uint64_t m, const uint32_t *offs,
 // would keep results exact; the bound keeps the build at one pass.
 constexpr uint32_t kRepScan = 256;
 __global__ void k_build_rep(const uint32_t *__restrict__ ioffs, const uint32_t *__restrict__ icols,
-                            const uint32_t *__restrict__ offs, uint32_t n, uint32_t *rep) {
+                            const uint32_t *__restrict__ offs, uint32_t n, uint2 *rep) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nw) {
@@ -366,7 +369,9 @@ __global__ void k_build_rep(const uint32_t *__restrict__ ioffs, const uint32_t *
       const unsigned long long t = __shfl_xor_sync(0xffffffffu, best, o);
       best = t > best ? t : best;
     }
-    if (lane == 0) rep[v] = best ? icols[b + (0xFFFFFFFFu - (uint32_t)best)] : kNoRep;
+    if (lane == 0)
+      rep[v] = make_uint2(best ? icols[b + (0xFFFFFFFFu - (uint32_t)best)] : kNoRep,
+                          offs[v + 1] - offs[v]);
   }
 }
 
@@ -376,9 +381,9 @@ int build_rep_locked(grus_graph *g) {
   const uint32_t *io = sym ? g->csr.offs : g->csc.offs;
   const uint32_t *ic = sym ? g->csr.cols : g->csc.cols;
   if (!io) return GRUS_EINVAL;
-  uint32_t *rep = nullptr;
+  uint2 *rep = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  cudaError_t e = cudaMalloc(&rep, std::max<uint64_t>(g->n, 1) * 4);
+  cudaError_t e = cudaMalloc(&rep, std::max<uint64_t>(g->n, 1) * sizeof(uint2));
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
   float ms = 0.f;

@@ -54,9 +54,10 @@ struct grus_graph {
   grus::Csr csr;              // out-edges
   grus::Csr csc;              // in-edges (built on demand; aliases csr if symmetric)
   uint32_t max_deg_vertex = 0, max_deg = 0;
-  // BFS pull index: per vertex, an in-neighbour of high out-degree (built on
-  // demand, grus::build_rep_locked), kNoRep without in-edges
-  uint32_t *bfs_rep = nullptr;
+  // BFS pull index: per vertex {an in-neighbour of high out-degree (kNoRep
+  // without in-edges), the vertex's out-degree}, built on demand
+  // (grus::build_rep_locked)
+  uint2 *bfs_rep = nullptr;
   float bfs_rep_ms = 0.f;
   grus_tuning tuning{};       // zero fields = library defaults
   std::mutex mu;              // guards the workspaces and the csc build

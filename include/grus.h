@@ -163,11 +163,12 @@ GRUS_API int grus_graph_from_csr(uint64_t n, uint64_t m, const uint32_t *offsets
                         grus_graph **out);
 /* Builds the BFS pull index of g ahead of its first BFS (grus_bfs builds it
  * on demand otherwise) and reports the device time it took.  No counterpart
- * in the reference.  Per vertex, one in-neighbour of high out-degree (4 bytes
- * per vertex, freed with the graph; built from the CSC on a directed graph,
- * which it builds too): a pull level tests that neighbour's frontier bit
- * before reading the vertex's adjacency, which settles nearly every vertex
- * found at the level without the scattered read.  Results do not change. */
+ * in the reference.  Per vertex, one in-neighbour of high out-degree and the
+ * vertex's out-degree (8 bytes per vertex, freed with the graph; built from
+ * the CSC on a directed graph, which it builds too): a pull level tests that
+ * neighbour's frontier bit before reading the vertex's adjacency, which
+ * settles nearly every vertex found at the level without the scattered read.
+ * Results do not change. */
 GRUS_API int grus_graph_build_index(grus_graph *g, float *build_ms);
 /* Load a Galois v1 .gr file.  Replaces graph_loader::Load
  * (include/graph_loader.cuh:160-166) + Set_Mem_Policy
