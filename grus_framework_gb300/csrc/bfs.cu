@@ -1368,7 +1368,7 @@ extern "C" int grus_bfs(grus_graph *g, uint32_t src, uint32_t *depth,
     attrs[nattr].id = cudaLaunchAttributeAccessPolicyWindow;
     attrs[nattr].val.accessPolicyWindow.base_ptr = w->bitmaps;
     attrs[nattr].val.accessPolicyWindow.num_bytes = (size_t)win;
-    attrs[nattr].val.accessPolicyWindow.hitRatio = 1.0f;
+    attrs[nattr].val.accessPolicyWindow.hitRatio = l2_hit_ratio((size_t)win);
     attrs[nattr].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
     attrs[nattr].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     ++nattr;

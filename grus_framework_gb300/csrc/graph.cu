@@ -498,6 +498,21 @@ int l2_window(cudaStream_t, void *, size_t bytes) {
   return (int)std::min<size_t>(bytes, (size_t)max_window);
 }
 
+float l2_hit_ratio(size_t bytes) {
+  static int p = -1;
+  if (p < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxPersistingL2CacheSize, dev) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    p = v;
+  }
+  if (p <= 0 || bytes <= (size_t)p) return 1.0f;
+  return (float)((double)p / (double)bytes);
+}
+
 }  // namespace grus
 
 using namespace grus;
@@ -875,7 +890,7 @@ int launch_persistent(const void *fn, void **args, int block, int per_sm_req,
     attrs[nattr].id = cudaLaunchAttributeAccessPolicyWindow;
     attrs[nattr].val.accessPolicyWindow.base_ptr = win_base;
     attrs[nattr].val.accessPolicyWindow.num_bytes = (size_t)win;
-    attrs[nattr].val.accessPolicyWindow.hitRatio = 1.0f;
+    attrs[nattr].val.accessPolicyWindow.hitRatio = l2_hit_ratio((size_t)win);
     attrs[nattr].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
     attrs[nattr].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     ++nattr;

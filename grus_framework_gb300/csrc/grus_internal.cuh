@@ -71,6 +71,10 @@ int graph_alloc_array(grus_graph *g, void **p, size_t bytes);
 void graph_free_array(grus_graph *g, void *p);
 int device_sm_count();
 int l2_window(cudaStream_t s, void *base, size_t bytes);
+// Share of a window of `bytes` that may persist: 1, or the persisting L2
+// set-aside over the window when the window is larger (persisting lines
+// beyond the set-aside would only evict one another).
+float l2_hit_ratio(size_t bytes);
 int build_csc_locked(grus_graph *g);
 // Builds g->bfs_rep for the graph's in-edges (the CSR of a symmetric graph,
 // else the CSC, which must exist); no-op when built.  Caller holds g->mu.
