@@ -81,7 +81,7 @@ struct LevelSlot {
   uint32_t scount;         // pull: vertices left unresolved, with in-edges
   unsigned long long mf;   // sum of their out-degrees
   uint32_t dcount;         // pull with the index: vertices it left to probe
-  uint32_t pad2;
+  uint32_t fcount;         // pull over a queue: vertices found, queued from the top
 };
 
 struct Summary {
@@ -566,7 +566,7 @@ __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, co
                                                    uint32_t *fnext, const uint32_t *sin,
                                                    uint32_t S, uint32_t &nf, unsigned long long &mf,
                                                    uint32_t *sq, uint32_t *scount,
-                                                   bool use_rep = true) {
+                                                   uint32_t *fcount, bool use_rep = true) {
   const uint32_t nd = L + 1;
   const uint32_t lane = lane_id();
   const uint32_t scan = a.bu_scan;
@@ -687,6 +687,30 @@ __device__ __forceinline__ void bu_level_survivors(const Args &a, uint32_t L, co
         base += __popc(m[k]);
       }
     }
+    // the vertices found, from the top of the same queue downwards: every
+    // vertex this level finds comes through here, so a push level next reads
+    // them from there instead of converting the frontier bitmap
+    if (fcount) {
+      tot = 0;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        m[k] = __ballot_sync(0xffffffffu, act[k] && found[k]);
+        tot += __popc(m[k]);
+      }
+      if (tot) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(fcount, tot);
+        base = __shfl_sync(0xffffffffu, base, 0);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          if ((m[k] >> lane) & 1u) {
+            const uint32_t at = base + __popc(m[k] & ((1u << lane) - 1u));
+            if (at < a.queue_cap) sq[a.queue_cap - 1 - at] = v[k];
+          }
+          base += __popc(m[k]);
+        }
+      }
+    }
   }
 }
 
@@ -788,6 +812,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
 
   uint32_t L = 0;
   bool bu = false, from_pull = false;
+  bool fq = false;  // the previous level queued every vertex it found (pull over a queue)
   // Survivors of the previous pull level: 0 none, 1 a bitmap in the words
   // this level writes as its next frontier (cleared before use), 2 a queue in
   // queue[L & 1] of S entries.
@@ -816,18 +841,27 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
     if (gtid < sizeof(LevelSlot) / 4) ((uint32_t *)(a.slots + ((L + 2) & 3u)))[gtid] = 0u;
     uint32_t nf = 0;
     unsigned long long mf = 0;
+    bool qpass = false;  // this pull level ran over a queue only
     if (!bu) {
       PushVisitor<P> vis{&a, L + 1, fnext, a.queue[(L + 1) & 1u], a.chunks[(L + 1) & 1u], nx, 0u, 0ull};
-      if (from_pull) {
-        bitmap_to_queue(a, fcur, a.queue[L & 1u], &cur->qcount);
-        // survivors recorded as a bitmap sit in this level's next frontier
-        if (surv == 1)
-          for (uint32_t i = gtid; i < a.W; i += nthreads) fnext[i] = 0u;
-        if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+      const uint32_t *q = a.queue[L & 1u];
+      uint32_t qc;
+      if (from_pull && fq) {
+        // the pull level queued what it found at the top of this queue
+        qc = min(__ldcg(&cur->fcount), a.queue_cap);
+        q += a.queue_cap - qc;
+      } else {
+        if (from_pull) {
+          bitmap_to_queue(a, fcur, a.queue[L & 1u], &cur->qcount);
+          // survivors recorded as a bitmap sit in this level's next frontier
+          if (surv == 1)
+            for (uint32_t i = gtid; i < a.W; i += nthreads) fnext[i] = 0u;
+          if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
+        }
+        qc = min(__ldcg(&cur->qcount), a.queue_cap);
       }
-      const uint32_t qc = min(__ldcg(&cur->qcount), a.queue_cap);
       const uint32_t cc = min(__ldcg(&cur->ccount), a.chunk_cap);
-      expand_binned<kBlock>(a.offs, a.queue[L & 1u], qc, a.chunks[L & 1u], cc, vis);
+      expand_binned<kBlock>(a.offs, q, qc, a.chunks[L & 1u], cc, vis);
       nf = vis.nf;
       mf = vis.mf;
     } else {
@@ -850,7 +884,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
         if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
         const uint32_t D = min(__ldcg(&nx->dcount), a.queue_cap);
         bu_level_survivors<K, P>(a, L, fcur, fnext, a.queue[L & 1u], D, nf, mf,
-                              a.queue[(L + 1) & 1u], &nx->scount, false);
+                              a.queue[(L + 1) & 1u], &nx->scount, nullptr, false);
       } else if (surv == 0) {
         uint32_t ns = 0;
         bu_level<K, P>(a, L, fcur, fnext, nf, mf, fclr, ns);
@@ -865,7 +899,8 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
           S = min(__ldcg(&cur->qcount), a.queue_cap);
         }
         bu_level_survivors<K, P>(a, L, fcur, fnext, a.queue[L & 1u], S, nf, mf,
-                              a.queue[(L + 1) & 1u], &nx->scount);
+                              a.queue[(L + 1) & 1u], &nx->scount, &nx->fcount);
+        qpass = true;
       }
     }
     const unsigned long long bnf = block_sum_u64<kBlock>(nf);
@@ -927,6 +962,7 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
       return;
     }
     from_pull = bu && !nbu;
+    fq = bu && qpass;
     // a push level after a word-based pull level still clears the bitmap
     surv = !bu ? 0 : (surv == 0 && !(a.rep && P) ? 1 : 2);
     if (!nbu && surv == 2) surv = 0;
