@@ -789,24 +789,41 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent(Args a) {
   const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
   const uint32_t nthreads = gridDim.x * kBlock;
   if (gtid == 0 && a.trace) a.trace[0] = LevelTrace{global_timer_ns(), 0ull, 1u, 0u};
-  // prologue: clear the bitmaps and the level slots
+  // prologue: clear the bitmaps and the level slots, and seed the source as
+  // the clearing goes (its visited and frontier bits, and level 0's work in
+  // slot 0: one queue entry, or its chunks written by as many threads, as
+  // push_binned bins it), so one grid barrier ends the prologue
+  const uint32_t sb = __ldg(a.offs + a.src), se = __ldg(a.offs + a.src + 1);
   {
+    const uint32_t sw = a.src >> 5, sbit = 1u << (a.src & 31u);
+    const uint32_t fw = (uint32_t)(a.front[0] - a.visited) + sw;
+    const uint32_t d = se - sb;
+    const bool chunked = d >= a.huge;
+    const uint32_t nch = chunked ? (d + kChunk - 1) / kChunk : 0u;
     uint32_t *bm = a.visited;
     const uint32_t words = (uint32_t)(a.front[2] - a.visited) + a.W;
-    for (uint32_t i = gtid; i < words; i += nthreads) bm[i] = 0u;
+    for (uint32_t i = gtid; i < words; i += nthreads) bm[i] = (i == sw || i == fw) ? sbit : 0u;
     if (P)
       for (uint32_t i = gtid; i < a.W; i += nthreads) a.planes[i] = 0u;
-    if (gtid < 4 * sizeof(LevelSlot) / 4) ((uint32_t *)a.slots)[gtid] = 0u;
-    if (gtid == 0 && a.ho) a.ho->flag = 0u;
-  }
-  if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
-  const uint32_t sb = __ldg(a.offs + a.src), se = __ldg(a.offs + a.src + 1);
-  if (gtid == 0) {
-    const uint32_t w = a.src >> 5, bit = 1u << (a.src & 31u);
-    a.visited[w] = bit;
-    a.front[0][w] = bit;
-    a.depth[a.src] = 0;
-    enqueue_binned(a, a.src, a.queue[0], a.chunks[0], a.slots);
+    if (gtid < 4 * sizeof(LevelSlot) / 4) {
+      uint32_t val = 0u;
+      if (gtid == offsetof(LevelSlot, qcount) / 4 && d > 0 && !chunked) val = 1u;
+      if (gtid == offsetof(LevelSlot, ccount) / 4 && chunked && nch <= a.chunk_cap) val = nch;
+      ((uint32_t *)a.slots)[gtid] = val;
+    }
+    if (chunked) {
+      if (nch > a.chunk_cap) {
+        if (gtid == 0) atomicOr(a.err, kErrOverflow);
+      } else {
+        for (uint32_t c = gtid; c < nch; c += nthreads)
+          a.chunks[0][c] = make_uint4(a.src, sb + c * kChunk, min(se, sb + (c + 1) * kChunk), 0u);
+      }
+    }
+    if (gtid == 0) {
+      if (a.ho) a.ho->flag = 0u;
+      if (!P) a.depth[a.src] = 0;
+      if (d > 0 && !chunked) a.queue[0][0] = a.src;
+    }
   }
   if (!grid_sync(a.bar, a.err, a.timeout_ns)) return;
 
