@@ -1,6 +1,6 @@
 """CPU: the reference's samples compile and link UNCHANGED against the mgg
 drop-in headers (grus_framework_gb300/mgg) and libgrus.so -- the drop-in
-contract of the template/operator API.  The samples are
+contract of the template/operator API (include/*.cuh, samples/*).  The samples are
 read from the Grus source tree where it is present (build container); the
 test is skipped elsewhere.  The repository's own drop-in test program is
 compiled too."""
