@@ -489,10 +489,13 @@ __device__ __forceinline__ void bu_level(const Args &a, uint32_t L, const uint32
   }
 }
 
-// First pull level with the pull index: each unvisited vertex tests only its
-// representative in-neighbour (one coalesced load and one frontier bit), so a
-// warp step never waits on adjacency reads.  Vertices it leaves unresolved
-// that have in-edges are marked in `dbm` (one plain store per word by the
+// First pull level with the pull index (graphs in the planes form): each
+// unvisited vertex tests only its representative in-neighbour (one
+// coalesced 8-byte index entry and one frontier bit), so a warp step never
+// waits on adjacency reads.  Of the vertices it leaves unresolved, those of
+// in-degree one on a symmetric graph are next level's survivors already
+// (their one in-neighbour is the representative) and are marked in
+// `a.aux`; the others are marked in `dbm` (one plain store per word by the
 // warp that owns it) and probed afterwards from a dense queue by
 // bu_level_survivors: with the probes of the few unresolved lanes removed
 // from the word pass, its steps no longer wait on the adjacency reads of one
